@@ -1,0 +1,88 @@
+"""K3 binning + K4 rasteriser on the GPU against the CPU oracle's per-quad rasteriser.
+
+With GS300_EXACT_EXP=1 the kernel evaluates exp with the same portable sequence as the oracle,
+and frames must match bit for bit (every fragment, every 8-bit re-quantisation).  With the
+default SFU exp (ex2.approx) frames must be within 1/255 per channel on >= 99.9% of pixels
+with PSNR >= 45 dB against the oracle — the frame tolerance of the render path."""
+import numpy as np
+import pytest
+
+from gpu_helpers import StagePipeline, frame_psnr, uniforms, within_one_fraction
+from gs300 import records as R
+from gs300 import scene as S
+
+pytestmark = pytest.mark.gpu
+
+MODES = [R.DISPLAY_SPLAT, R.DISPLAY_ELLIPSE, R.DISPLAY_POINT]
+
+
+def _oracle_frame(oracle, u, sc, fmt, w, h, exp_mode, threads=8):
+    img, *_ = oracle.render(u, sc, fmt, w, h, exp_mode=exp_mode, threads=threads)
+    return img
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("n,w,h", [(3000, 200, 120), (40_000, 333, 197)])
+def test_frame_bit_exact_with_portable_exp(gs, cuda, oracle, monkeypatch, mode, n, w, h):
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(n, seed=21)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, w, h)
+    for k in (0, 50):
+        u = uniforms(gs, w, h, k=k, mode=mode, radius=5.0)
+        got = pipe.render(u)
+        want = _oracle_frame(oracle, u, sc, R.FORMAT_FP32, w, h, exp_mode=0, threads=0 if n < 5000 else 8)
+        assert np.array_equal(got, want), f"{(got != want).any(axis=-1).sum()} pixels differ"
+        st, pairs = gs.Renderer.status(pipe.r_scratch)
+        assert st == 0 and pairs > 0
+
+
+def test_frame_bit_exact_tiny_and_ragged_targets(gs, cuda, oracle, monkeypatch):
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(2000, seed=22)
+    for w, h in ((1, 1), (17, 3), (15, 33), (64, 16)):
+        pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, w, h)
+        u = uniforms(gs, w, h, k=3, radius=4.0)
+        assert np.array_equal(pipe.render(u), _oracle_frame(oracle, u, sc, R.FORMAT_FP32, w, h, 0, threads=0))
+
+
+def test_frame_fast_exp_small_config(gs, cuda, oracle):
+    """Plain small configuration: 100k Gaussians, 1280x720, splat mode."""
+    sc = S.synth_scene(100_000, seed=0)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, 1280, 720)
+    u = uniforms(gs, 1280, 720, k=0)
+    got = pipe.render(u)
+    want = _oracle_frame(oracle, u, sc, R.FORMAT_FP32, 1280, 720, exp_mode=1)
+    assert within_one_fraction(got, want) >= 0.999
+    assert frame_psnr(got, want) >= 45.0
+    assert (got[..., 3] == 255).all()
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_frame_full_config_all_modes(gs, cuda, oracle, mode):
+    """Plain full-scale configuration: 1M Gaussians, 1920x1080, splat + ellipse + point frames."""
+    sc = S.synth_scene(1_000_000, seed=1)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, 1920, 1080)
+    u = uniforms(gs, 1920, 1080, k=17, mode=mode)
+    got = pipe.render(u)
+    want = _oracle_frame(oracle, u, sc, R.FORMAT_FP32, 1920, 1080, exp_mode=1, threads=16)
+    assert within_one_fraction(got, want) >= 0.999
+    assert frame_psnr(got, want) >= 45.0
+    st, _ = gs.Renderer.status(pipe.r_scratch)
+    assert st == 0
+
+
+def test_pair_overflow_is_reported(gs, cuda):
+    sc = S.synth_scene(20_000, seed=23)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, 320, 180, max_pairs=1000)
+    pipe.render(uniforms(gs, 320, 180, k=1))
+    st, pairs = gs.Renderer.status(pipe.r_scratch)
+    assert st == 6 and pairs > 1000  # GS_ERR_CAPACITY with the wanted count
+
+
+def test_repeated_frames_identical(gs, cuda):
+    sc = S.synth_scene(50_000, seed=24)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, 640, 360)
+    u = uniforms(gs, 640, 360, k=9)
+    a = pipe.render(u)
+    for _ in range(3):
+        assert np.array_equal(pipe.render(u), a)

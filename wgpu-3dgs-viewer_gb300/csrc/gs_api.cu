@@ -1,0 +1,934 @@
+// gs_api.cu — the C ABI (include/gs300.h): host-side camera/transform math, stage entry points
+// over caller-owned device buffers, and the Viewer / MultiModelViewer facades.
+//
+// Host FP32 math is compiled with -ffp-contract=off and follows the evaluation order of the
+// kernels, so frame uniforms built here are bit-identical to the oracle's.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gs300.h"
+#include "gs_internal.h"
+
+using namespace gs;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gs_status fail(gs_status s, const char *fmt, ...) __attribute__((format(printf, 2, 3)));
+gs_status fail(gs_status s, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+gs_status cuda_fail(cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(GS_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    }
+    return fail(GS_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define GS_CUDA(call)                                      \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// ---- host FP32 linear algebra (column-major), same order as the kernels ----
+void mat4_mul(const float *a, const float *b, float *out) {
+    float t[16];
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            float s = a[0 * 4 + r] * b[c * 4 + 0];
+            s = s + a[1 * 4 + r] * b[c * 4 + 1];
+            s = s + a[2 * 4 + r] * b[c * 4 + 2];
+            s = s + a[3 * 4 + r] * b[c * 4 + 3];
+            t[c * 4 + r] = s;
+        }
+    std::memcpy(out, t, sizeof(t));
+}
+
+void mat3_mul(const float *a, const float *b, float *out) {
+    float t[9];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) {
+            float s = a[0 * 3 + r] * b[c * 3 + 0];
+            s = s + a[1 * 3 + r] * b[c * 3 + 1];
+            s = s + a[2 * 3 + r] * b[c * 3 + 2];
+            t[c * 3 + r] = s;
+        }
+    std::memcpy(out, t, sizeof(t));
+}
+
+void quat_to_mat3(const float *q, float *m) {
+    const float x = q[0], y = q[1], z = q[2], w = q[3];
+    const float x2 = x + x, y2 = y + y, z2 = z + z;
+    const float xx = x * x2, xy = x * y2, xz = x * z2;
+    const float yy = y * y2, yz = y * z2, zz = z * z2;
+    const float wx = w * x2, wy = w * y2, wz = w * z2;
+    m[0] = 1.0f - (yy + zz);
+    m[1] = xy + wz;
+    m[2] = xz - wy;
+    m[3] = xy - wz;
+    m[4] = 1.0f - (xx + zz);
+    m[5] = yz + wx;
+    m[6] = xz + wy;
+    m[7] = yz - wx;
+    m[8] = 1.0f - (xx + yy);
+}
+
+size_t record_bytes(uint32_t format) {
+    return format == GS_FORMAT_FP32 ? sizeof(gs_gaussian_pod) : sizeof(gs_gaussian_pod_half);
+}
+
+bool valid_format(uint32_t f) {
+    return f == GS_FORMAT_FP32 || f == GS_FORMAT_HALF_SH_FP16 || f == GS_FORMAT_HALF_SH_BF16;
+}
+
+gs_status check_gaussian_transform(const gs_gaussian_transform_pod *p) {
+    if (!p) return fail(GS_ERR_INVALID_ARG, "gaussian transform pod is NULL");
+    if (p->display_mode > GS_DISPLAY_POINT)
+        return fail(GS_ERR_INVALID_ARG, "display mode %u is not splat/ellipse/point", p->display_mode);
+    if (p->sh_deg > 3) return fail(GS_ERR_INVALID_ARG, "SH degree %u out of range 0..=3", p->sh_deg);
+    if (!(p->max_std_dev >= 0.0f && p->max_std_dev <= 3.0f))
+        return fail(GS_ERR_INVALID_ARG, "max std dev %g out of range 0..=3", (double)p->max_std_dev);
+    return GS_OK;
+}
+
+bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
+// Device allocation owned by a facade.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes && ptr) return cudaSuccess;
+        release();
+        cudaError_t e = cudaMalloc(&ptr, b ? b : 256);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+};
+
+gs_status status_from_bits(uint32_t bits, const char *what) {
+    if (bits & kStatusTimeout) return fail(GS_ERR_TIMEOUT, "%s: a bounded device wait gave up", what);
+    if (bits & kStatusCapacity) return fail(GS_ERR_CAPACITY, "%s: tile-pair list exceeded its capacity", what);
+    return GS_OK;
+}
+
+uint32_t default_pairs(uint32_t n, uint32_t w, uint32_t h) {
+    uint64_t p = (uint64_t)n * 8u + (uint64_t)((w + 15) / 16) * ((h + 15) / 16) * 4u + 4096u;
+    if (p > 0x7FFFFFFFull) p = 0x7FFFFFFFull;
+    return (uint32_t)p;
+}
+
+// Per-model device state shared by both facades.
+struct Model {
+    uint32_t n = 0, format = GS_FORMAT_FP32;
+    DevBuf records, control, indices, depths, splats, pre_scratch, sort_scratch, selection;
+    int invert = 0;
+    bool has_selection = false;
+    gs_model_transform_pod model{};
+    uint32_t *indirect() { return reinterpret_cast<uint32_t *>(control.ptr); }  // [0..4) args, [4..7) dispatch
+
+    gs_status create(const void *host, uint32_t count, uint32_t fmt) {
+        if (!valid_format(fmt)) return fail(GS_ERR_INVALID_ARG, "unknown record format %u", fmt);
+        if (count > 0 && !host) return fail(GS_ERR_INVALID_ARG, "records pointer is NULL");
+        n = count;
+        format = fmt;
+        model = gs_model_transform_pod{};
+        model.rot[3] = 1.0f;
+        model.scale[0] = model.scale[1] = model.scale[2] = 1.0f;
+        const size_t rb = record_bytes(fmt);
+        GS_CUDA(records.ensure((size_t)n * rb));
+        if (n) GS_CUDA(cudaMemcpy(records.ptr, host, (size_t)n * rb, cudaMemcpyHostToDevice));
+        GS_CUDA(control.ensure(64));
+        GS_CUDA(cudaMemset(control.ptr, 0, 64));
+        GS_CUDA(indices.ensure((size_t)n * 4));
+        GS_CUDA(depths.ensure((size_t)gs_depth_capacity(n) * 4));
+        GS_CUDA(splats.ensure((size_t)n * sizeof(gs_splat)));
+        GS_CUDA(pre_scratch.ensure(preprocess_scratch_bytes(n)));
+        GS_CUDA(cudaMemset(pre_scratch.ptr, 0, pre_scratch.bytes));
+        GS_CUDA(sort_scratch.ensure(sort_scratch_bytes(n, 32)));
+        GS_CUDA(cudaMemset(sort_scratch.ptr, 0, sort_scratch.bytes));
+        return GS_OK;
+    }
+
+    // Preprocess + depth sort of this model for one frame.
+    gs_status enqueue(const gs_frame_uniforms &u, cudaStream_t st) {
+        cudaError_t e = launch_preprocess(u, records.ptr, format, n,
+                                          has_selection ? (const uint32_t *)selection.ptr : nullptr, invert,
+                                          indirect(), indirect() + 4, (uint32_t *)indices.ptr, (float *)depths.ptr,
+                                          gs_depth_capacity(n), (gs_splat *)splats.ptr, pre_scratch.ptr, st);
+        if (e != cudaSuccess) return cuda_fail(e, "preprocess launch");
+        e = launch_sort((uint32_t *)depths.ptr, (uint32_t *)indices.ptr, n, indirect() + 1, 32, sort_scratch.ptr, st);
+        if (e != cudaSuccess) return cuda_fail(e, "sort launch");
+        return GS_OK;
+    }
+
+    gs_status set_selection(const uint32_t *bits, int inv) {
+        if (!bits) {
+            has_selection = false;
+            return GS_OK;
+        }
+        const size_t words = ((size_t)n + 31) / 32;
+        GS_CUDA(selection.ensure(words * 4 + 4));
+        if (words) GS_CUDA(cudaMemcpy(selection.ptr, bits, words * 4, cudaMemcpyHostToDevice));
+        has_selection = true;
+        invert = inv;
+        return GS_OK;
+    }
+
+    uint32_t device_status() {
+        Ctrl a{}, b{};
+        if (pre_scratch.ptr) cudaMemcpy(&a, pre_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost);
+        if (sort_scratch.ptr) cudaMemcpy(&b, sort_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost);
+        return a.status | b.status;
+    }
+};
+
+// Shared render state: camera/Gaussian-transform pods, raster scratch and last-frame args.
+struct Frame {
+    gs_camera_pod camera{};
+    gs_gaussian_transform_pod gt{};
+    DevBuf raster_scratch;
+    uint32_t max_pairs = 0, scratch_splats = 0, scratch_w = 0, scratch_h = 0;
+    uint8_t *last_target = nullptr;
+    uint32_t last_w = 0, last_h = 0, last_pitch = 0;
+    bool rendered = false;
+    int exact_exp = 0;
+
+    Frame() {
+        gt.size = 1.0f;
+        gt.display_mode = GS_DISPLAY_SPLAT;
+        gt.sh_deg = 3;
+        gt.no_sh0 = 0;
+        gt.max_std_dev = 3.0f;
+    }
+
+    gs_status ensure_scratch(uint32_t splats, uint32_t w, uint32_t h) {
+        if (max_pairs == 0) max_pairs = default_pairs(splats, w, h);
+        if (raster_scratch.ptr && splats <= scratch_splats && w == scratch_w && h == scratch_h) return GS_OK;
+        const size_t b = raster_scratch_bytes(splats, w, h, max_pairs);
+        raster_scratch.release();
+        GS_CUDA(raster_scratch.ensure(b));
+        GS_CUDA(cudaMemset(raster_scratch.ptr, 0, b));
+        scratch_splats = splats;
+        scratch_w = w;
+        scratch_h = h;
+        return GS_OK;
+    }
+
+    gs_status grow_pairs(uint32_t wanted) {
+        uint64_t p = (uint64_t)wanted + wanted / 4 + 4096;
+        if (p > 0x7FFFFFFFull) p = 0x7FFFFFFFull;
+        if (p <= max_pairs) return fail(GS_ERR_CAPACITY, "tile-pair list cannot grow beyond %u", max_pairs);
+        max_pairs = (uint32_t)p;
+        raster_scratch.release();
+        return ensure_scratch(scratch_splats, scratch_w, scratch_h);
+    }
+};
+
+gs_status check_target(const uint8_t *target, uint32_t w, uint32_t h, uint32_t pitch) {
+    if (!target) return fail(GS_ERR_INVALID_ARG, "target is NULL");
+    if (w == 0 || h == 0) return fail(GS_ERR_INVALID_ARG, "target size %ux%u is empty", w, h);
+    if (pitch < 4u * w || pitch % 4u != 0 || !aligned(target, 4))
+        return fail(GS_ERR_INVALID_ARG, "target pitch %u / alignment invalid for width %u", pitch, w);
+    return GS_OK;
+}
+
+}  // namespace
+
+// ---- stage timers and launch counter ---------------------------------------------------------
+namespace gs {
+namespace {
+std::atomic<uint64_t> g_launches{0};
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+struct StageEvents {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;
+    size_t used = 0;
+    bool open = false;
+};
+StageEvents g_prof[kProfStages];
+}  // namespace
+
+void count_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+void prof_mark(int stage, bool begin, cudaStream_t st) {
+    if (!g_prof_on) return;
+    std::lock_guard<std::mutex> g(g_prof_mu);
+    StageEvents &e = g_prof[stage];
+    if (begin) {
+        if (e.used == e.pairs.size()) {
+            cudaEvent_t a, b;
+            if (cudaEventCreate(&a) != cudaSuccess) return;
+            if (cudaEventCreate(&b) != cudaSuccess) return;
+            e.pairs.emplace_back(a, b);
+        }
+        cudaEventRecord(e.pairs[e.used].first, st);
+        e.open = true;
+    } else if (e.open) {
+        cudaEventRecord(e.pairs[e.used].second, st);
+        ++e.used;
+        e.open = false;
+    }
+}
+}  // namespace gs
+
+// =============================================================================================
+extern "C" {
+
+const char *gs_last_error(void) { return g_last_error.c_str(); }
+const char *gs_version(void) { return "gs300 0.1.0 sm_103a"; }
+
+uint64_t gs_launch_count(void) { return gs::g_launches.load(); }
+
+gs_status gs_profile_enable(int enable) {
+    std::lock_guard<std::mutex> g(gs::g_prof_mu);
+    for (auto &e : gs::g_prof) {
+        e.used = 0;
+        e.open = false;
+    }
+    gs::g_prof_on = enable != 0;
+    return GS_OK;
+}
+
+gs_status gs_profile_read(double *ms, uint32_t *launches) {
+    GS_CUDA(cudaDeviceSynchronize());
+    std::lock_guard<std::mutex> g(gs::g_prof_mu);
+    for (int s = 0; s < gs::kProfStages; ++s) {
+        double acc = 0.0;
+        for (size_t i = 0; i < gs::g_prof[s].used; ++i) {
+            float t = 0.0f;
+            GS_CUDA(cudaEventElapsedTime(&t, gs::g_prof[s].pairs[i].first, gs::g_prof[s].pairs[i].second));
+            acc += t;
+        }
+        if (ms) ms[s] = acc;
+        if (launches) launches[s] = (uint32_t)gs::g_prof[s].used;
+    }
+    return GS_OK;
+}
+
+gs_status gs_camera_view(const gs_camera *c, float out[16]) {
+    if (!c || !out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    const float f[3] = {std::cos(c->pitch) * std::sin(c->yaw), std::sin(c->pitch), std::cos(c->pitch) * std::cos(c->yaw)};
+    // look_to_rh(eye, dir, up = +Y)
+    float l = std::sqrt((f[0] * f[0] + f[1] * f[1]) + f[2] * f[2]);
+    const float fn[3] = {f[0] / l, f[1] / l, f[2] / l};
+    const float up[3] = {0.0f, 1.0f, 0.0f};
+    float s[3] = {fn[1] * up[2] - fn[2] * up[1], fn[2] * up[0] - fn[0] * up[2], fn[0] * up[1] - fn[1] * up[0]};
+    l = std::sqrt((s[0] * s[0] + s[1] * s[1]) + s[2] * s[2]);
+    s[0] = s[0] / l;
+    s[1] = s[1] / l;
+    s[2] = s[2] / l;
+    const float u[3] = {s[1] * fn[2] - s[2] * fn[1], s[2] * fn[0] - s[0] * fn[2], s[0] * fn[1] - s[1] * fn[0]};
+    const float *e = c->pos;
+    const float m[16] = {s[0], u[0], -fn[0], 0.0f, s[1], u[1], -fn[1], 0.0f, s[2], u[2], -fn[2], 0.0f,
+                         -((e[0] * s[0] + e[1] * s[1]) + e[2] * s[2]),
+                         -((e[0] * u[0] + e[1] * u[1]) + e[2] * u[2]),
+                         (e[0] * fn[0] + e[1] * fn[1]) + e[2] * fn[2], 1.0f};
+    std::memcpy(out, m, sizeof(m));
+    return GS_OK;
+}
+
+gs_status gs_camera_projection(const gs_camera *c, float aspect, float out[16]) {
+    if (!c || !out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    const float half = 0.5f * c->vertical_fov;
+    const float h = std::cos(half) / std::sin(half);
+    const float w = h / aspect;
+    const float r = c->z_far / (c->z_near - c->z_far);
+    std::memset(out, 0, 16 * sizeof(float));
+    out[0] = w;
+    out[5] = h;
+    out[10] = r;
+    out[11] = -1.0f;
+    out[14] = r * c->z_near;
+    return GS_OK;
+}
+
+gs_status gs_camera_pod_new(const gs_camera *c, uint32_t w, uint32_t h, gs_camera_pod *pod) {
+    if (!c || !pod || w == 0 || h == 0) return fail(GS_ERR_INVALID_ARG, "invalid camera pod arguments");
+    std::memset(pod, 0, sizeof(*pod));
+    gs_camera_view(c, pod->view);
+    gs_camera_projection(c, (float)w / (float)h, pod->proj);
+    pod->size[0] = (float)w;
+    pod->size[1] = (float)h;
+    return GS_OK;
+}
+
+gs_status gs_gaussian_transform_pod_new(float size, uint32_t mode, uint32_t sh_deg, int no_sh0, float std_dev,
+                                        gs_gaussian_transform_pod *out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    gs_gaussian_transform_pod p{};
+    p.size = size;
+    p.display_mode = mode;
+    p.sh_deg = sh_deg;
+    p.no_sh0 = no_sh0 ? 1u : 0u;
+    p.max_std_dev = std_dev;
+    const gs_status s = check_gaussian_transform(&p);
+    if (s != GS_OK) return s;
+    *out = p;
+    return GS_OK;
+}
+
+gs_status gs_model_transform_pod_new(const float pos[3], const float rot[4], const float scale[3],
+                                     gs_model_transform_pod *out) {
+    if (!pos || !rot || !scale || !out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    gs_model_transform_pod p{};
+    std::memcpy(p.pos, pos, 12);
+    std::memcpy(p.rot, rot, 16);
+    std::memcpy(p.scale, scale, 12);
+    *out = p;
+    return GS_OK;
+}
+
+gs_status gs_gaussian_pack(const gs_gaussian *g, size_t count, gs_gaussian_pod *out) {
+    if (count && (!g || !out)) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    for (size_t i = 0; i < count; ++i) {
+        gs_gaussian_pod &o = out[i];
+        std::memset(&o, 0, sizeof(o));
+        std::memcpy(o.pos, g[i].pos, 12);
+        o.color = (uint32_t)g[i].color[0] | ((uint32_t)g[i].color[1] << 8) | ((uint32_t)g[i].color[2] << 16) |
+                  ((uint32_t)g[i].color[3] << 24);
+        std::memcpy(o.sh, g[i].sh, sizeof(o.sh));
+        // Σ = (R·S)(R·S)ᵀ, accumulated in double and rounded once.
+        const double x = g[i].rot[0], y = g[i].rot[1], z = g[i].rot[2], w = g[i].rot[3];
+        const double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)},
+                                {2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)},
+                                {2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)}};
+        double M[3][3];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) M[r][c] = R[r][c] * (double)g[i].scale[c];
+        auto cv = [&](int a, int b) { return (float)(M[a][0] * M[b][0] + M[a][1] * M[b][1] + M[a][2] * M[b][2]); };
+        o.cov3d[0] = cv(0, 0);
+        o.cov3d[1] = cv(0, 1);
+        o.cov3d[2] = cv(0, 2);
+        o.cov3d[3] = cv(1, 1);
+        o.cov3d[4] = cv(1, 2);
+        o.cov3d[5] = cv(2, 2);
+    }
+    return GS_OK;
+}
+
+gs_status gs_frame_uniforms_build(const gs_camera_pod *cam, const gs_model_transform_pod *mt,
+                                  const gs_gaussian_transform_pod *gt, uint32_t vw, uint32_t vh,
+                                  gs_frame_uniforms *u) {
+    if (!cam || !mt || !u) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    const gs_status s = check_gaussian_transform(gt);
+    if (s != GS_OK) return s;
+    std::memset(u, 0, sizeof(*u));
+    mat4_mul(cam->proj, cam->view, u->pv);
+    float R[9], SR[9];
+    quat_to_mat3(mt->rot, R);
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) SR[c * 3 + r] = R[c * 3 + r] * mt->scale[c];
+    for (int c = 0; c < 3; ++c) {
+        for (int r = 0; r < 3; ++r) u->model[c * 4 + r] = SR[c * 3 + r];
+        u->model[c * 4 + 3] = 0.0f;
+    }
+    u->model[12] = mt->pos[0];
+    u->model[13] = mt->pos[1];
+    u->model[14] = mt->pos[2];
+    u->model[15] = 1.0f;
+    mat4_mul(cam->view, u->model, u->vm);
+    float Wm[9];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) Wm[c * 3 + r] = cam->view[c * 4 + r];
+    mat3_mul(Wm, SR, u->wsr);
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) u->inv_sr[c * 3 + r] = R[r * 3 + c] / mt->scale[r];
+    const float *t = cam->view + 12;
+    for (int i = 0; i < 3; ++i)
+        u->cam_pos[i] = -((Wm[i * 3 + 0] * t[0] + Wm[i * 3 + 1] * t[1]) + Wm[i * 3 + 2] * t[2]);
+    u->size[0] = cam->size[0];
+    u->size[1] = cam->size[1];
+    u->focal[0] = (cam->proj[0] * cam->size[0]) * 0.5f;
+    u->focal[1] = (cam->proj[5] * cam->size[1]) * 0.5f;
+    u->viewport[0] = (float)vw;
+    u->viewport[1] = (float)vh;
+    u->std_dev = gt->max_std_dev;
+    u->std_dev_scaled = gt->max_std_dev * gt->size;
+    u->point_size = gt->size;
+    u->display_mode = gt->display_mode;
+    u->sh_deg = gt->sh_deg;
+    u->no_sh0 = gt->no_sh0;
+    return GS_OK;
+}
+
+// ---- stage entry points ----------------------------------------------------------------
+uint32_t gs_depth_capacity(uint32_t n) {
+    const uint64_t c = ((uint64_t)n + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS * GS_SORT_BLOCK_KVS;
+    return c > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)c;
+}
+
+size_t gs_preprocess_scratch_bytes(uint32_t n) { return preprocess_scratch_bytes(n); }
+
+gs_status gs_preprocess(const gs_frame_uniforms *u, const void *gaussians, uint32_t format, uint32_t n,
+                        const uint32_t *selection, int invert, uint32_t *indirect, uint32_t *dispatch,
+                        uint32_t *indices, float *depths, uint32_t depth_cap, gs_splat *splats, void *scratch,
+                        size_t scratch_bytes, gs_stream stream) {
+    if (!u) return fail(GS_ERR_INVALID_ARG, "uniforms are NULL");
+    if (!valid_format(format)) return fail(GS_ERR_INVALID_ARG, "unknown record format %u", format);
+    if (n && (!gaussians || !indices || !depths)) return fail(GS_ERR_INVALID_ARG, "NULL buffer");
+    if (n && !aligned(gaussians, 16)) return fail(GS_ERR_INVALID_ARG, "records must be 16-byte aligned");
+    if (splats && !aligned(splats, 16)) return fail(GS_ERR_INVALID_ARG, "splats must be 16-byte aligned");
+    if (depth_cap < n) return fail(GS_ERR_INVALID_ARG, "depth capacity %u < n %u", depth_cap, n);
+    if (!scratch || scratch_bytes < preprocess_scratch_bytes(n))
+        return fail(GS_ERR_INVALID_ARG, "scratch smaller than gs_preprocess_scratch_bytes(n)");
+    const cudaError_t e = launch_preprocess(*u, gaussians, format, n, selection, invert, indirect, dispatch,
+                                            indices, depths, depth_cap, splats, scratch, (cudaStream_t)stream);
+    return e == cudaSuccess ? GS_OK : cuda_fail(e, "gs_preprocess");
+}
+
+size_t gs_radix_sort_scratch_bytes(uint32_t max_count) { return sort_scratch_bytes(max_count, 32); }
+
+gs_status gs_radix_sort(uint32_t *keys, uint32_t *values, uint32_t max_count, const uint32_t *count,
+                        uint32_t key_bits, void *scratch, size_t scratch_bytes, gs_stream stream) {
+    if (key_bits < 1 || key_bits > 32) return fail(GS_ERR_INVALID_ARG, "key_bits %u not in 1..=32", key_bits);
+    if (max_count && (!keys || !values)) return fail(GS_ERR_INVALID_ARG, "NULL buffer");
+    if (!scratch || scratch_bytes < sort_scratch_bytes(max_count, key_bits))
+        return fail(GS_ERR_INVALID_ARG, "scratch smaller than gs_radix_sort_scratch_bytes(max_count)");
+    const cudaError_t e = launch_sort(keys, values, max_count, count, key_bits, scratch, (cudaStream_t)stream);
+    return e == cudaSuccess ? GS_OK : cuda_fail(e, "gs_radix_sort");
+}
+
+size_t gs_rasterize_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_t max_pairs) {
+    return raster_scratch_bytes(max_splats, w, h, max_pairs);
+}
+
+gs_status gs_rasterize(const gs_frame_uniforms *u, const gs_splat *splats, const uint32_t *sorted, const uint32_t *count,
+                       uint32_t max_splats, uint8_t *target, uint32_t w, uint32_t h, uint32_t pitch, uint32_t max_pairs,
+                       void *scratch, size_t scratch_bytes, gs_stream stream) {
+    if (!u) return fail(GS_ERR_INVALID_ARG, "uniforms are NULL");
+    gs_status s = check_target(target, w, h, pitch);
+    if (s != GS_OK) return s;
+    if (max_splats && (!splats || !sorted)) return fail(GS_ERR_INVALID_ARG, "NULL buffer");
+    if (splats && !aligned(splats, 16)) return fail(GS_ERR_INVALID_ARG, "splats must be 16-byte aligned");
+    if (!scratch || scratch_bytes < raster_scratch_bytes(max_splats, w, h, max_pairs))
+        return fail(GS_ERR_INVALID_ARG, "scratch smaller than gs_rasterize_scratch_bytes");
+    const RasterSegment seg{splats, sorted, count, max_splats};
+    const int exact = getenv("GS300_EXACT_EXP") ? 1 : 0;
+    const cudaError_t e = launch_raster(&seg, 1, *u, target, w, h, pitch, max_pairs, scratch, exact, (cudaStream_t)stream);
+    return e == cudaSuccess ? GS_OK : cuda_fail(e, "gs_rasterize");
+}
+
+gs_status gs_scratch_status(const void *scratch, gs_stream stream, uint32_t *pairs) {
+    if (!scratch) return fail(GS_ERR_INVALID_ARG, "scratch is NULL");
+    GS_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    Ctrl c{};
+    GS_CUDA(cudaMemcpy(&c, scratch, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+    if (pairs) *pairs = c.total;
+    return status_from_bits(c.status, "stage");
+}
+
+// ---- Viewer -------------------------------------------------------------------------------
+}  // extern "C"
+
+struct gs_viewer {
+    Model model;
+    Frame frame;
+    std::mutex mu;
+};
+
+struct gs_target {
+    DevBuf buf;
+    uint32_t w = 0, h = 0;
+};
+
+namespace {
+
+gs_status viewer_render_locked(gs_viewer *v, uint8_t *target, uint32_t w, uint32_t h, uint32_t pitch,
+                               cudaStream_t st) {
+    gs_status s = check_target(target, w, h, pitch);
+    if (s != GS_OK) return s;
+    s = v->frame.ensure_scratch(v->model.n, w, h);
+    if (s != GS_OK) return s;
+    gs_frame_uniforms u;
+    s = gs_frame_uniforms_build(&v->frame.camera, &v->model.model, &v->frame.gt, w, h, &u);
+    if (s != GS_OK) return s;
+    s = v->model.enqueue(u, st);
+    if (s != GS_OK) return s;
+    const RasterSegment seg{(const gs_splat *)v->model.splats.ptr, (const uint32_t *)v->model.indices.ptr,
+                            v->model.indirect() + 1, v->model.n};
+    const cudaError_t e = launch_raster(&seg, 1, u, target, w, h, pitch, v->frame.max_pairs, v->frame.raster_scratch.ptr,
+                                        v->frame.exact_exp, st);
+    if (e != cudaSuccess) return cuda_fail(e, "raster launch");
+    v->frame.last_target = target;
+    v->frame.last_w = w;
+    v->frame.last_h = h;
+    v->frame.last_pitch = pitch;
+    v->frame.rendered = true;
+    return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gs_status gs_viewer_create(const void *host_records, uint32_t count, uint32_t format, gs_viewer **out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "out is NULL");
+    gs_viewer *v = new gs_viewer();
+    const gs_status s = v->model.create(host_records, count, format);
+    if (s != GS_OK) {
+        delete v;
+        return s;
+    }
+    v->frame.exact_exp = getenv("GS300_EXACT_EXP") ? 1 : 0;
+    *out = v;
+    return GS_OK;
+}
+
+void gs_viewer_destroy(gs_viewer *v) {
+    if (!v) return;
+    cudaDeviceSynchronize();
+    delete v;
+}
+
+uint32_t gs_viewer_len(const gs_viewer *v) { return v ? v->model.n : 0; }
+
+gs_status gs_viewer_update_camera(gs_viewer *v, const gs_camera *c, uint32_t w, uint32_t h) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return gs_camera_pod_new(c, w, h, &v->frame.camera);
+}
+
+gs_status gs_viewer_update_camera_with_pod(gs_viewer *v, const gs_camera_pod *pod) {
+    if (!v || !pod) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(v->mu);
+    v->frame.camera = *pod;
+    return GS_OK;
+}
+
+gs_status gs_viewer_update_model_transform(gs_viewer *v, const float pos[3], const float rot[4], const float scale[3]) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return gs_model_transform_pod_new(pos, rot, scale, &v->model.model);
+}
+
+gs_status gs_viewer_update_model_transform_with_pod(gs_viewer *v, const gs_model_transform_pod *pod) {
+    if (!v || !pod) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(v->mu);
+    v->model.model = *pod;
+    return GS_OK;
+}
+
+gs_status gs_viewer_update_gaussian_transform(gs_viewer *v, float size, uint32_t mode, uint32_t sh_deg, int no_sh0,
+                                              float std_dev) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return gs_gaussian_transform_pod_new(size, mode, sh_deg, no_sh0, std_dev, &v->frame.gt);
+}
+
+gs_status gs_viewer_update_gaussian_transform_with_pod(gs_viewer *v, const gs_gaussian_transform_pod *pod) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    const gs_status s = check_gaussian_transform(pod);
+    if (s != GS_OK) return s;
+    std::lock_guard<std::mutex> g(v->mu);
+    v->frame.gt = *pod;
+    return GS_OK;
+}
+
+gs_status gs_viewer_set_selection(gs_viewer *v, const uint32_t *bits, int invert) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return v->model.set_selection(bits, invert);
+}
+
+gs_status gs_viewer_render(gs_viewer *v, uint8_t *target, uint32_t w, uint32_t h, uint32_t pitch, gs_stream stream) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return viewer_render_locked(v, target, w, h, pitch, (cudaStream_t)stream);
+}
+
+gs_status gs_viewer_synchronize(gs_viewer *v, gs_stream stream) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        GS_CUDA(cudaStreamSynchronize(st));
+        if (!v->frame.rendered) return GS_OK;
+        Ctrl c{};
+        GS_CUDA(cudaMemcpy(&c, v->frame.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+        const uint32_t bits = c.status | v->model.device_status();
+        if (bits & kStatusTimeout) return status_from_bits(bits, "render");
+        if (!(bits & kStatusCapacity)) return GS_OK;
+        gs_status s = v->frame.grow_pairs(c.total);
+        if (s != GS_OK) return s;
+        s = viewer_render_locked(v, v->frame.last_target, v->frame.last_w, v->frame.last_h, v->frame.last_pitch, st);
+        if (s != GS_OK) return s;
+    }
+    return fail(GS_ERR_CAPACITY, "tile-pair list kept overflowing");
+}
+
+gs_status gs_viewer_stats(gs_viewer *v, gs_stream stream, uint32_t *visible, uint32_t *pairs) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    GS_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    uint32_t args[4] = {0, 0, 0, 0};
+    GS_CUDA(cudaMemcpy(args, v->model.control.ptr, sizeof(args), cudaMemcpyDeviceToHost));
+    Ctrl c{};
+    if (v->frame.raster_scratch.ptr) GS_CUDA(cudaMemcpy(&c, v->frame.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+    if (visible) *visible = args[1];
+    if (pairs) *pairs = c.total;
+    return GS_OK;
+}
+
+gs_status gs_viewer_buffers(gs_viewer *v, uint32_t **indices, float **depths, uint32_t **indirect, gs_splat **splats) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    if (indices) *indices = (uint32_t *)v->model.indices.ptr;
+    if (depths) *depths = (float *)v->model.depths.ptr;
+    if (indirect) *indirect = v->model.indirect();
+    if (splats) *splats = (gs_splat *)v->model.splats.ptr;
+    return GS_OK;
+}
+
+// ---- targets --------------------------------------------------------------------------------
+gs_status gs_target_create(uint32_t w, uint32_t h, gs_target **out) {
+    if (!out || w == 0 || h == 0) return fail(GS_ERR_INVALID_ARG, "invalid target arguments");
+    gs_target *t = new gs_target();
+    const cudaError_t e = t->buf.ensure((size_t)w * h * 4);
+    if (e != cudaSuccess) {
+        delete t;
+        return cuda_fail(e, "target allocation");
+    }
+    t->w = w;
+    t->h = h;
+    *out = t;
+    return GS_OK;
+}
+
+void gs_target_destroy(gs_target *t) {
+    if (!t) return;
+    cudaDeviceSynchronize();
+    delete t;
+}
+
+uint8_t *gs_target_data(gs_target *t) { return t ? (uint8_t *)t->buf.ptr : nullptr; }
+uint32_t gs_target_pitch(const gs_target *t) { return t ? t->w * 4 : 0; }
+
+gs_status gs_target_download(gs_target *t, uint8_t *host, gs_stream stream) {
+    if (!t || !host) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    GS_CUDA(cudaMemcpyAsync(host, t->buf.ptr, (size_t)t->w * t->h * 4, cudaMemcpyDeviceToHost, st));
+    GS_CUDA(cudaStreamSynchronize(st));
+    return GS_OK;
+}
+
+}  // extern "C"
+
+// ---- MultiModelViewer -----------------------------------------------------------------------
+struct gs_multi_viewer {
+    std::map<std::string, Model *> models;
+    Frame frame;
+    std::mutex mu;
+    std::vector<std::string> last_keys;
+    ~gs_multi_viewer() {
+        for (auto &kv : models) delete kv.second;
+    }
+};
+
+namespace {
+
+gs_status multi_render_locked(gs_multi_viewer *v, const std::vector<std::string> &keys, uint8_t *target, uint32_t w,
+                              uint32_t h, uint32_t pitch, cudaStream_t st) {
+    gs_status s = check_target(target, w, h, pitch);
+    if (s != GS_OK) return s;
+    std::vector<Model *> ms;
+    for (const auto &k : keys) {
+        auto it = v->models.find(k);
+        if (it == v->models.end()) return fail(GS_ERR_NOT_FOUND, "model '%s' not found", k.c_str());
+        ms.push_back(it->second);
+    }
+    uint64_t total = 0;
+    for (Model *m : ms) total += m->n;
+    if (total > 0xFFFFFFFFull) return fail(GS_ERR_INVALID_ARG, "too many Gaussians in one render");
+    s = v->frame.ensure_scratch((uint32_t)total, w, h);
+    if (s != GS_OK) return s;
+    std::vector<RasterSegment> segs;
+    gs_frame_uniforms u{};
+    for (Model *m : ms) {
+        s = gs_frame_uniforms_build(&v->frame.camera, &m->model, &v->frame.gt, w, h, &u);
+        if (s != GS_OK) return s;
+        s = m->enqueue(u, st);
+        if (s != GS_OK) return s;
+        segs.push_back(RasterSegment{(const gs_splat *)m->splats.ptr, (const uint32_t *)m->indices.ptr, m->indirect() + 1, m->n});
+    }
+    if (ms.empty()) {
+        gs_model_transform_pod identity{};
+        identity.rot[3] = 1.0f;
+        identity.scale[0] = identity.scale[1] = identity.scale[2] = 1.0f;
+        s = gs_frame_uniforms_build(&v->frame.camera, &identity, &v->frame.gt, w, h, &u);
+        if (s != GS_OK) return s;
+    }
+    // The raster only reads viewport, std dev and display mode, which all models share.
+    const cudaError_t e = launch_raster(segs.data(), (uint32_t)segs.size(), u, target, w, h, pitch, v->frame.max_pairs,
+                                        v->frame.raster_scratch.ptr, v->frame.exact_exp, st);
+    if (e != cudaSuccess) return cuda_fail(e, "raster launch");
+    v->last_keys = keys;
+    v->frame.last_target = target;
+    v->frame.last_w = w;
+    v->frame.last_h = h;
+    v->frame.last_pitch = pitch;
+    v->frame.rendered = true;
+    return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gs_status gs_multi_viewer_create(gs_multi_viewer **out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "out is NULL");
+    gs_multi_viewer *v = new gs_multi_viewer();
+    v->frame.exact_exp = getenv("GS300_EXACT_EXP") ? 1 : 0;
+    *out = v;
+    return GS_OK;
+}
+
+void gs_multi_viewer_destroy(gs_multi_viewer *v) {
+    if (!v) return;
+    cudaDeviceSynchronize();
+    delete v;
+}
+
+gs_status gs_multi_viewer_insert_model(gs_multi_viewer *v, const char *key, const void *host, uint32_t count,
+                                       uint32_t format) {
+    if (!v || !key) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    Model *m = new Model();
+    const gs_status s = m->create(host, count, format);
+    if (s != GS_OK) {
+        delete m;
+        return s;
+    }
+    std::lock_guard<std::mutex> g(v->mu);
+    auto it = v->models.find(key);
+    if (it != v->models.end()) {
+        cudaDeviceSynchronize();
+        delete it->second;
+        it->second = m;
+    } else {
+        v->models.emplace(key, m);
+    }
+    return GS_OK;
+}
+
+gs_status gs_multi_viewer_remove_model(gs_multi_viewer *v, const char *key) {
+    if (!v || !key) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(v->mu);
+    auto it = v->models.find(key);
+    if (it == v->models.end()) return fail(GS_ERR_NOT_FOUND, "model '%s' not found", key);
+    cudaDeviceSynchronize();
+    delete it->second;
+    v->models.erase(it);
+    return GS_OK;
+}
+
+uint32_t gs_multi_viewer_model_count(const gs_multi_viewer *v) { return v ? (uint32_t)v->models.size() : 0; }
+
+gs_status gs_multi_viewer_update_camera(gs_multi_viewer *v, const gs_camera *c, uint32_t w, uint32_t h) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return gs_camera_pod_new(c, w, h, &v->frame.camera);
+}
+
+gs_status gs_multi_viewer_update_camera_with_pod(gs_multi_viewer *v, const gs_camera_pod *pod) {
+    if (!v || !pod) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(v->mu);
+    v->frame.camera = *pod;
+    return GS_OK;
+}
+
+gs_status gs_multi_viewer_update_model_transform(gs_multi_viewer *v, const char *key, const float pos[3],
+                                                 const float rot[4], const float scale[3]) {
+    if (!v || !key) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(v->mu);
+    auto it = v->models.find(key);
+    if (it == v->models.end()) return fail(GS_ERR_NOT_FOUND, "model '%s' not found", key);
+    return gs_model_transform_pod_new(pos, rot, scale, &it->second->model);
+}
+
+gs_status gs_multi_viewer_update_model_transform_with_pod(gs_multi_viewer *v, const char *key,
+                                                          const gs_model_transform_pod *pod) {
+    if (!v || !key || !pod) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(v->mu);
+    auto it = v->models.find(key);
+    if (it == v->models.end()) return fail(GS_ERR_NOT_FOUND, "model '%s' not found", key);
+    it->second->model = *pod;
+    return GS_OK;
+}
+
+gs_status gs_multi_viewer_update_gaussian_transform(gs_multi_viewer *v, float size, uint32_t mode, uint32_t sh_deg,
+                                                    int no_sh0, float std_dev) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    return gs_gaussian_transform_pod_new(size, mode, sh_deg, no_sh0, std_dev, &v->frame.gt);
+}
+
+gs_status gs_multi_viewer_update_gaussian_transform_with_pod(gs_multi_viewer *v, const gs_gaussian_transform_pod *pod) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    const gs_status s = check_gaussian_transform(pod);
+    if (s != GS_OK) return s;
+    std::lock_guard<std::mutex> g(v->mu);
+    v->frame.gt = *pod;
+    return GS_OK;
+}
+
+gs_status gs_multi_viewer_render(gs_multi_viewer *v, const char *const *keys, uint32_t key_count, uint8_t *target,
+                                 uint32_t w, uint32_t h, uint32_t pitch, gs_stream stream) {
+    if (!v || (key_count && !keys)) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::vector<std::string> ks;
+    for (uint32_t i = 0; i < key_count; ++i) {
+        if (!keys[i]) return fail(GS_ERR_INVALID_ARG, "key %u is NULL", i);
+        ks.emplace_back(keys[i]);
+    }
+    std::lock_guard<std::mutex> g(v->mu);
+    return multi_render_locked(v, ks, target, w, h, pitch, (cudaStream_t)stream);
+}
+
+gs_status gs_multi_viewer_synchronize(gs_multi_viewer *v, gs_stream stream) {
+    if (!v) return fail(GS_ERR_INVALID_ARG, "viewer is NULL");
+    std::lock_guard<std::mutex> g(v->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        GS_CUDA(cudaStreamSynchronize(st));
+        if (!v->frame.rendered) return GS_OK;
+        Ctrl c{};
+        GS_CUDA(cudaMemcpy(&c, v->frame.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+        uint32_t bits = c.status;
+        for (const auto &k : v->last_keys) {
+            auto it = v->models.find(k);
+            if (it != v->models.end()) bits |= it->second->device_status();
+        }
+        if (bits & kStatusTimeout) return status_from_bits(bits, "render");
+        if (!(bits & kStatusCapacity)) return GS_OK;
+        gs_status s = v->frame.grow_pairs(c.total);
+        if (s != GS_OK) return s;
+        s = multi_render_locked(v, v->last_keys, v->frame.last_target, v->frame.last_w, v->frame.last_h,
+                                v->frame.last_pitch, st);
+        if (s != GS_OK) return s;
+    }
+    return fail(GS_ERR_CAPACITY, "tile-pair list kept overflowing");
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// gs_common.cuh — device-side helpers shared by the preprocess, sort and raster kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gs_record.h"
+
+namespace gs {
+
+// Sticky error bits of a scratch area's control block.
+constexpr uint32_t kStatusTimeout = 1u;
+constexpr uint32_t kStatusCapacity = 2u;
+
+// Upper bound on polls of a look-back flag or an mbarrier before a kernel gives up, records
+// kStatusTimeout and carries on with a garbage value (so that waiting successors also end).
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Control block at the start of every scratch area.  `epoch` is bumped by the stage's init
+// kernel; look-back flags written under an older epoch read as "not yet published", so the
+// flag arrays never need clearing.
+struct Ctrl {
+    uint32_t epoch;
+    uint32_t status;
+    uint32_t ticket[8];
+    uint32_t count;       // preprocess: V; raster: tile pairs kept
+    uint32_t total;       // raster: tile pairs wanted (saturating)
+    uint32_t pair_base;   // raster: running pair offset across segments
+    uint32_t pad[3];
+    uint32_t hist[4][256];  // sort: global digit histograms
+};
+static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl must keep 16-byte alignment of what follows");
+
+// Look-back flag word: epoch (30 bits) | status (2 bits) | value (32 bits).
+constexpr uint32_t kFlagAggregate = 1u;
+constexpr uint32_t kFlagPrefix = 2u;
+
+__device__ __forceinline__ uint64_t pack_flag(uint32_t epoch, uint32_t status, uint32_t value) {
+    return ((uint64_t)epoch << 34) | ((uint64_t)status << 32) | (uint64_t)value;
+}
+
+__device__ __forceinline__ void st_release(uint64_t *p, uint64_t v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
+    uint64_t v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Exclusive look-back over predecessors j = tile-1 .. 0 of one counter whose flags live at
+// flags[j * stride].  Returns the exclusive prefix; on timeout sets the status bit.
+__device__ __forceinline__ uint32_t look_back(const uint64_t *flags, uint32_t stride, uint32_t tile,
+                                              uint32_t epoch, uint32_t *status) {
+    uint32_t prefix = 0;
+    int64_t j = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+        const uint64_t w = ld_acquire(flags + (uint64_t)j * stride);
+        const uint32_t ep = (uint32_t)(w >> 34);
+        const uint32_t st = (uint32_t)(w >> 32) & 3u;
+        if (ep != epoch || st == 0u) {
+            if (++spins > kSpinLimit) {
+                atomicOr(status, kStatusTimeout);
+                break;
+            }
+            if (spins > 64) __nanosleep(32);
+            continue;
+        }
+        prefix += (uint32_t)w;
+        if (st == kFlagPrefix) break;
+        --j;
+    }
+    return prefix;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Round to nearest even for |x| < 2^22 with two IEEE adds (no conversion instruction).
+__device__ __forceinline__ float rint_small(float x) {
+    const float m = 12582912.0f;
+    return __fsub_rn(__fadd_rn(x, m), m);
+}
+
+// exp(x) on [-10, 0]: Cody–Waite reduction with the classic two-part ln2, degree-7 Taylor
+// polynomial in Horner form with FMAs, scale by 2^k through the exponent field.  The CPU
+// oracle evaluates the identical sequence, so the two agree bit for bit.
+__device__ __forceinline__ float exp_portable(float x) {
+    const float k = rint_small(__fmul_rn(x, 1.44269504088896341f));
+    float r = fmaf(-k, 0.693359375f, x);
+    r = fmaf(-k, -2.12194440e-4f, r);
+    float p = 1.0f / 5040.0f;
+    p = fmaf(p, r, 1.0f / 720.0f);
+    p = fmaf(p, r, 1.0f / 120.0f);
+    p = fmaf(p, r, 1.0f / 24.0f);
+    p = fmaf(p, r, 1.0f / 6.0f);
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = fmaf(p, r, 1.0f);
+    const int ki = (int)k;
+    return __fmul_rn(p, __uint_as_float((uint32_t)(ki + 127) << 23));
+}
+
+// Scratch carving: 256-byte aligned sub-allocations.
+__host__ __device__ __forceinline__ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace gs

@@ -1,0 +1,51 @@
+// gs_internal.h — declarations shared between the kernel translation units and the C ABI.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "gs_common.cuh"
+#include "gs_record.h"
+
+namespace gs {
+
+// Stage timers (CUDA events on the launching stream; recorded only while profiling is on) and
+// the count of kernels this library has launched.
+enum ProfStage { kProfPreprocess = 0, kProfDepthSort, kProfBin, kProfTileSort, kProfRanges, kProfRaster, kProfStages };
+void prof_mark(int stage, bool begin, cudaStream_t st);
+void count_launches(uint32_t n);
+
+// Resets a control block: mode 1 = a new stage call (epoch, status, tickets, counters,
+// histograms); mode 0 = a new segment inside a call (epoch and ticket[0] only).
+__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode);
+
+// ---- K1 preprocess (gs_preprocess.cu) ----
+size_t preprocess_scratch_bytes(uint32_t n);
+cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, uint32_t format,
+                              uint32_t n, const uint32_t *selection, int invert, uint32_t *indirect,
+                              uint32_t *dispatch, uint32_t *indices, float *depths,
+                              uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st);
+
+// ---- K2 onesweep radix sort (gs_sort.cu) ----
+size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits);
+cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
+                        uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage = kProfDepthSort);
+
+// ---- K3 binning + K4 raster (gs_raster.cu) ----
+struct RasterSegment {
+    const gs_splat *splats;       // indexed by Gaussian index
+    const uint32_t *sorted_index; // draw order
+    const uint32_t *count;        // device: number of entries in sorted_index
+    uint32_t max_count;           // capacity of sorted_index
+};
+size_t raster_scratch_bytes(uint32_t max_splats, uint32_t width, uint32_t height, uint32_t max_pairs);
+// exact_exp: 1 = the portable exp (bit-identical with the CPU oracle), 0 = the SFU exp.
+cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u,
+                          uint8_t *target, uint32_t width, uint32_t height, uint32_t pitch,
+                          uint32_t max_pairs, void *scratch, int exact_exp, cudaStream_t st);
+// Scratch control block of a raster call (status, pair counts).
+const Ctrl *raster_ctrl(const void *scratch);
+
+}  // namespace gs

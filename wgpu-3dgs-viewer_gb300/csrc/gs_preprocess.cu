@@ -1,0 +1,554 @@
+// gs_preprocess.cu — K1: fused preprocess (cull, depth key, order-preserving compaction,
+// screen-space splat: 2D axes -> pixel-to-quad map, SH colour).
+//
+// Restates src/shader/preprocess.wesl:52-126 (pre / main / post) and moves the per-instance
+// vertex work of src/shader/render.wesl:75-130 (cov2d_axes, view colour, quad geometry) here,
+// once per Gaussian instead of six times per splat.  Compiled with -fmad=false: every FP32
+// multiply and add rounds on its own, in the order of the CPU oracle (oracle/gs_oracle.cpp).
+//
+// Layout: a CTA owns 128 consecutive Gaussians.  One thread stages the CTA's records
+// (128 x 224 B = 28 KiB, or 128 x 128 B for the compressed record) into shared memory with a
+// single cp.async.bulk copy completing on an mbarrier, then each thread works on its record
+// from shared memory.  Visible Gaussians are compacted in ascending index order with a warp
+// ballot, a block scan and a decoupled look-back across CTAs (virtual CTA ids from a ticket).
+#include "gs_internal.h"
+
+namespace gs {
+
+constexpr uint32_t kPreThreads = 128;
+
+struct PreParams {
+    gs_frame_uniforms u;
+    const uint8_t *records;
+    uint32_t n;
+    uint32_t ntiles;
+    const uint32_t *selection;
+    uint32_t invert;
+    uint32_t *indirect;
+    uint32_t *dispatch;
+    uint32_t *indices;
+    float *depths;
+    uint32_t depth_cap;
+    gs_splat *splats;
+    Ctrl *ctrl;
+    uint64_t *flags;
+};
+
+// ---- FP32 math in the oracle's evaluation order ------------------------------------------
+__device__ __forceinline__ void mat4_vec(const float *m, const float *v, float *o) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float s = m[0 * 4 + r] * v[0];
+        s = s + m[1 * 4 + r] * v[1];
+        s = s + m[2 * 4 + r] * v[2];
+        s = s + m[3 * 4 + r] * v[3];
+        o[r] = s;
+    }
+}
+
+__device__ __forceinline__ void mat3_vec(const float *m, const float *v, float *o) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        float s = m[0 * 3 + r] * v[0];
+        s = s + m[1 * 3 + r] * v[1];
+        s = s + m[2 * 3 + r] * v[2];
+        o[r] = s;
+    }
+}
+
+__device__ __forceinline__ float minf_wgsl(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float clamp01(float v) { return v > 0.0f ? (v < 1.0f ? v : 1.0f) : 0.0f; }
+__device__ __forceinline__ float len2(float x, float y) { return sqrtf(x * x + y * y); }
+__device__ __forceinline__ bool cull(float x, float y, float z) {
+    return !(x >= -1.0f && y >= -1.0f && z >= 0.0f && x <= 1.0f && y <= 1.0f && z <= 1.0f);
+}
+
+// Unpacked record (FP32 values regardless of the stored format).
+struct Rec {
+    float pos[3];
+    uint32_t color;
+    const float *sh32;      // FP32 record: SH in shared memory
+    const uint16_t *sh16;   // compressed record: SH bits in shared memory
+    float cov3d[6];
+};
+
+template <uint32_t FMT>
+__device__ __forceinline__ float sh_at(const Rec &g, int k) {
+    if constexpr (FMT == GS_FORMAT_FP32) {
+        return g.sh32[k];
+    } else if constexpr (FMT == GS_FORMAT_HALF_SH_FP16) {
+        return __half2float(__ushort_as_half(g.sh16[k]));
+    } else {
+        return __uint_as_float((uint32_t)g.sh16[k] << 16);
+    }
+}
+
+__device__ __forceinline__ void quat_to_mat3(const float *q, float *m) {
+    const float x = q[0], y = q[1], z = q[2], w = q[3];
+    const float x2 = x + x, y2 = y + y, z2 = z + z;
+    const float xx = x * x2, xy = x * y2, xz = x * z2;
+    const float yy = y * y2, yz = y * z2, zz = z * z2;
+    const float wx = w * x2, wy = w * y2, wz = w * z2;
+    m[0] = 1.0f - (yy + zz);
+    m[1] = xy + wz;
+    m[2] = xz - wy;
+    m[3] = xy - wz;
+    m[4] = 1.0f - (xx + zz);
+    m[5] = yz + wx;
+    m[6] = xz + wy;
+    m[7] = yz - wx;
+    m[8] = 1.0f - (xx + yy);
+}
+
+template <uint32_t FMT>
+__device__ __forceinline__ Rec load_rec(const uint8_t *s) {
+    Rec g;
+    if constexpr (FMT == GS_FORMAT_FP32) {
+        const gs_gaussian_pod *p = reinterpret_cast<const gs_gaussian_pod *>(s);
+        g.pos[0] = p->pos[0];
+        g.pos[1] = p->pos[1];
+        g.pos[2] = p->pos[2];
+        g.color = p->color;
+        g.sh32 = p->sh;
+        g.sh16 = nullptr;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) g.cov3d[k] = p->cov3d[k];
+    } else {
+        const gs_gaussian_pod_half *p = reinterpret_cast<const gs_gaussian_pod_half *>(s);
+        g.pos[0] = p->pos[0];
+        g.pos[1] = p->pos[1];
+        g.pos[2] = p->pos[2];
+        g.color = p->color;
+        g.sh32 = nullptr;
+        g.sh16 = p->sh;
+        float q[4], sc[3];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) q[k] = __half2float(__ushort_as_half(p->rot[k]));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) sc[k] = __half2float(__ushort_as_half(p->scale[k]));
+        const float nrm = sqrtf(((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) q[k] = q[k] / nrm;
+        float R[9], M[9];
+        quat_to_mat3(q, R);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+            for (int r = 0; r < 3; ++r) M[c * 3 + r] = R[c * 3 + r] * sc[c];
+        auto cv = [&](int a, int b) {
+            float acc = M[0 * 3 + a] * M[0 * 3 + b];
+            acc = acc + M[1 * 3 + a] * M[1 * 3 + b];
+            acc = acc + M[2 * 3 + a] * M[2 * 3 + b];
+            return acc;
+        };
+        g.cov3d[0] = cv(0, 0);
+        g.cov3d[1] = cv(0, 1);
+        g.cov3d[2] = cv(0, 2);
+        g.cov3d[3] = cv(1, 1);
+        g.cov3d[4] = cv(1, 2);
+        g.cov3d[5] = cv(2, 2);
+    }
+    return g;
+}
+
+// cov2d (utils.wesl:25-48) + cov2d_axes (utils.wesl:54-79): (major.xy, minor.xy).
+__device__ __forceinline__ void cov2d_axes(const gs_frame_uniforms &u, const float *c,
+                                           const float *p4, float std_dev, float *axes) {
+    float t[4];
+    mat4_vec(u.vm, p4, t);
+    const float fx = u.focal[0], fy = u.focal[1];
+    const float tz2 = t[2] * t[2];
+    const float j00 = fx / t[2];
+    const float j02 = -(fx * t[0]) / tz2;
+    const float j11 = fy / t[2];
+    const float j12 = -(fy * t[1]) / tz2;
+    const float *w = u.wsr;
+    float T0[3], T1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        T0[k] = j00 * w[k * 3 + 0] + j02 * w[k * 3 + 2];
+        T1[k] = j11 * w[k * 3 + 1] + j12 * w[k * 3 + 2];
+    }
+    const float V[9] = {c[0], c[1], c[2], c[1], c[3], c[4], c[2], c[4], c[5]};
+    float U0[3], U1[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        U0[k] = (T0[0] * V[k * 3 + 0] + T0[1] * V[k * 3 + 1]) + T0[2] * V[k * 3 + 2];
+        U1[k] = (T1[0] * V[k * 3 + 0] + T1[1] * V[k * 3 + 1]) + T1[2] * V[k * 3 + 2];
+    }
+    const float a = (U0[0] * T0[0] + U0[1] * T0[1]) + U0[2] * T0[2];
+    const float b = (U0[0] * T1[0] + U0[1] * T1[1]) + U0[2] * T1[2];
+    const float cc = (U1[0] * T1[0] + U1[1] * T1[1]) + U1[2] * T1[2];
+    const float mid = 0.5f * (a + cc);
+    const float h = 0.5f * (a - cc);
+    const float radius = len2(h, b);
+    const float lmaj = mid + radius;
+    const float lmin = mid - radius;
+    if (lmin < 0.0f) {
+        axes[0] = axes[1] = axes[2] = axes[3] = 0.0f;
+        return;
+    }
+    const float dx = b, dy = lmaj - a;
+    float dirx, diry;
+    if (dx == 0.0f && dy == 0.0f) {
+        dirx = 0.0f;
+        diry = 1.0f;
+    } else {
+        const float l = len2(dx, dy);
+        dirx = dx / l;
+        diry = dy / l;
+    }
+    const float majl = minf_wgsl(std_dev * sqrtf(lmaj), 1024.0f);
+    const float minl = minf_wgsl(std_dev * sqrtf(lmin), 1024.0f);
+    axes[0] = majl * dirx;
+    axes[1] = majl * diry;
+    axes[2] = minl * diry;
+    axes[3] = minl * -dirx;
+}
+
+// view_color (utils.wesl:82-135) with the direction of render.wesl:58-73.
+template <uint32_t FMT>
+__device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec &g,
+                                           const float *world, float *rgba) {
+    const float vd[3] = {u.cam_pos[0] - world[0], u.cam_pos[1] - world[1], u.cam_pos[2] - world[2]};
+    float mvd[3];
+    mat3_vec(u.inv_sr, vd, mvd);
+    const float l = sqrtf((mvd[0] * mvd[0] + mvd[1] * mvd[1]) + mvd[2] * mvd[2]);
+    const float x = -(mvd[0] / l), y = -(mvd[1] / l), z = -(mvd[2] / l);
+    const float c1 = 0.4886025f;
+    float res[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+        res[ch] = u.no_sh0 ? 0.5f : (float)((g.color >> (8 * ch)) & 0xFFu) / 255.0f;
+    if (u.sh_deg >= 1) {
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+            float v = (-sh_at<FMT>(g, 0 * 3 + ch)) * y + sh_at<FMT>(g, 1 * 3 + ch) * z;
+            v = v - sh_at<FMT>(g, 2 * 3 + ch) * x;
+            res[ch] = res[ch] + c1 * v;
+        }
+        if (u.sh_deg >= 2) {
+            const float xx = x * x, yy = y * y, zz = z * z;
+            const float xy = x * y, yz = y * z, xz = x * z;
+            const float k0 = 1.0925484f * xy, k1 = -1.0925484f * yz;
+            const float k2 = 0.3153916f * ((2.0f * zz - xx) - yy);
+            const float k3 = -1.0925484f * xz, k4 = 0.5462742f * (xx - yy);
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                float v = k0 * sh_at<FMT>(g, 3 * 3 + ch) + k1 * sh_at<FMT>(g, 4 * 3 + ch);
+                v = v + k2 * sh_at<FMT>(g, 5 * 3 + ch);
+                v = v + k3 * sh_at<FMT>(g, 6 * 3 + ch);
+                v = v + k4 * sh_at<FMT>(g, 7 * 3 + ch);
+                res[ch] = res[ch] + v;
+            }
+            if (u.sh_deg >= 3) {
+                const float m0 = (-0.5900436f * y) * (3.0f * xx - yy);
+                const float m1 = (2.8906114f * xy) * z;
+                const float m2 = (-0.4570458f * y) * ((4.0f * zz - xx) - yy);
+                const float m3 = (0.3731763f * z) * ((2.0f * zz - 3.0f * xx) - 3.0f * yy);
+                const float m4 = (-0.4570458f * x) * ((4.0f * zz - xx) - yy);
+                const float m5 = (1.4453057f * z) * (xx - yy);
+                const float m6 = (-0.5900436f * x) * (xx - 3.0f * yy);
+#pragma unroll
+                for (int ch = 0; ch < 3; ++ch) {
+                    float v = m0 * sh_at<FMT>(g, 8 * 3 + ch) + m1 * sh_at<FMT>(g, 9 * 3 + ch);
+                    v = v + m2 * sh_at<FMT>(g, 10 * 3 + ch);
+                    v = v + m3 * sh_at<FMT>(g, 11 * 3 + ch);
+                    v = v + m4 * sh_at<FMT>(g, 12 * 3 + ch);
+                    v = v + m5 * sh_at<FMT>(g, 13 * 3 + ch);
+                    v = v + m6 * sh_at<FMT>(g, 14 * 3 + ch);
+                    res[ch] = res[ch] + v;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) rgba[ch] = res[ch] > 0.0f ? res[ch] : 0.0f;
+    rgba[3] = (float)((g.color >> 24) & 0xFFu) / 255.0f;
+}
+
+// Fragment-bearing r² bound of a splat (see gs_splat.ex): a fragment with
+// alpha·exp(-r²) <= 1/512 cannot move an 8-bit channel; ln x <= ln2·(e + m - 1 + 0.0861).
+__device__ __forceinline__ float splat_r2_bound(float alpha, float std2) {
+    const float x = 512.0f * alpha;
+    if (!(x > 0.0f)) return -1.0f;
+    const uint32_t bits = __float_as_uint(x);
+    const float e = (float)((int)((bits >> 23) & 0xFFu) - 127);
+    const float mant = __uint_as_float((bits & 0x7FFFFFu) | 0x3F800000u);
+    const float r2 = 0.693147182f * (e + (mant - 1.0f) + 0.0862f) + 0.01f;
+    return minf_wgsl(std2, r2);
+}
+
+// ---- mbarrier + bulk copy (global -> shared) ----------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(bar);
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
+        "l"(src), "r"(bytes), "r"(b)
+        : "memory");
+}
+
+// Bounded wait for phase `parity` of the barrier; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
+    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <uint32_t FMT>
+__global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_constant__ PreParams P) {
+    constexpr uint32_t REC = (FMT == GS_FORMAT_FP32) ? 224u : 128u;
+    __shared__ __align__(128) uint8_t s_rec[kPreThreads * REC];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_tile, s_epoch, s_base, s_warp[kPreThreads / 32];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const gs_frame_uniforms &u = P.u;
+
+    if (tid == 0) {
+        s_epoch = *(volatile uint32_t *)&P.ctrl->epoch;
+        s_tile = atomicAdd(&P.ctrl->ticket[0], 1u);
+        mbar_init(&s_bar, 1);
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile, epoch = s_epoch;
+    const uint32_t first = tile * kPreThreads;
+    const uint32_t cnt = min(kPreThreads, P.n - first);
+    if (tid == 0) {
+        const uint32_t bytes = cnt * REC;
+        mbar_expect_tx(&s_bar, bytes);
+        bulk_g2s(s_rec, P.records + (size_t)first * REC, bytes, &s_bar);
+    }
+    if (!mbar_wait(&s_bar, 0)) atomicOr(&P.ctrl->status, kStatusTimeout);
+
+    const uint32_t i = first + tid;
+    bool vis = false;
+    float key = 0.0f, nx = 0.0f, ny = 0.0f, world[4], axes[4];
+    bool have_axes = false;
+    Rec g;
+    const float p4w = 1.0f;
+    if (tid < cnt) {
+        bool selected = true;
+        if (P.selection) {
+            const bool bit = (P.selection[i >> 5] >> (i & 31u)) & 1u;
+            selected = (P.invert != 0u) != bit;
+        }
+        if (selected) {
+            g = load_rec<FMT>(s_rec + (size_t)tid * REC);
+            const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
+            float clip[4];
+            mat4_vec(u.model, p4, world);
+            mat4_vec(u.pv, world, clip);
+            nx = clip[0] / clip[3];
+            ny = clip[1] / clip[3];
+            const float nz = clip[2] / clip[3];
+            vis = true;
+            if (cull(nx, ny, nz)) {
+                cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, axes);
+                have_axes = true;
+                const float mx = axes[0] * u.std_dev / u.size[0];
+                const float my = axes[1] * u.std_dev / u.size[1];
+                const float mlen = len2(mx, my);
+                const float nl = len2(nx, ny);
+                const float dx = -nx / nl, dy = -ny / nl;
+                const float m = minf_wgsl(mlen, nl);
+                if (cull(nx + m * dx, ny + m * dy, nz)) vis = false;
+            }
+            key = 1.0f - nz;
+        }
+    }
+
+    // ---- order-preserving compaction: ballot, block scan, decoupled look-back ----
+    const uint32_t bal = __ballot_sync(0xFFFFFFFFu, vis);
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t run = 0;
+        for (uint32_t w = 0; w < kPreThreads / 32; ++w) {
+            const uint32_t c = s_warp[w];
+            s_warp[w] = run;
+            run += c;
+        }
+        const uint32_t total = run;
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st_release(P.flags, pack_flag(epoch, kFlagPrefix, total));
+        } else {
+            st_release(P.flags + tile, pack_flag(epoch, kFlagAggregate, total));
+            prefix = look_back(P.flags, 1, tile, epoch, &P.ctrl->status);
+            st_release(P.flags + tile, pack_flag(epoch, kFlagPrefix, prefix + total));
+        }
+        s_base = prefix;
+        if (tile == P.ntiles - 1) {
+            // `post` (preprocess.wesl:108-126) and the DrawIndirectArgs instance count.
+            const uint32_t v = prefix + total;
+            P.ctrl->count = v;
+            if (P.indirect) {
+                P.indirect[0] = 6u;
+                P.indirect[1] = v;
+                P.indirect[2] = 0u;
+                P.indirect[3] = 0u;
+            }
+            if (P.dispatch) {
+                P.dispatch[0] = (v + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS;
+                P.dispatch[1] = 1u;
+                P.dispatch[2] = 1u;
+            }
+        }
+    }
+    __syncthreads();
+    if (tile == P.ntiles - 1) {
+        const uint32_t v = P.ctrl->count;
+        const uint32_t padded = min(((v + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS) * GS_SORT_BLOCK_KVS, P.depth_cap);
+        for (uint32_t k = v + tid; k < padded; k += kPreThreads) P.depths[k] = 2.0f;
+    }
+    if (!vis) return;
+    const uint32_t c = s_base + s_warp[warp] + __popc(bal & lanemask_lt());
+    P.indices[c] = i;
+    P.depths[c] = key;
+    if (!P.splats) return;
+
+    // ---- per-instance vertex work (render.wesl:75-130) ----
+    float rgba[4];
+    view_color<FMT>(u, g, world, rgba);
+    const float W = u.viewport[0], H = u.viewport[1];
+    const float cx = ((nx + 1.0f) * W) * 0.5f;
+    const float cy = ((1.0f - ny) * H) * 0.5f;
+    float q0, q1, q2, q3, ex, ey;
+    const float std2 = u.std_dev * u.std_dev;
+    const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
+    if (u.display_mode == GS_DISPLAY_POINT) {
+        float vp[4];
+        mat4_vec(u.vm, p4, vp);
+        const float l = sqrtf((vp[0] * vp[0] + vp[1] * vp[1]) + vp[2] * vp[2]);
+        const float aspect = u.size[1] / u.size[0];
+        const float pnd = (0.01f * u.point_size) / l;
+        const float hx = (pnd * aspect) * (0.5f * W);
+        const float hy = pnd * (0.5f * H);
+        q0 = hx;
+        q1 = hy;
+        q2 = 0.0f;
+        q3 = 0.0f;
+        if (hx > 0.0f && hy > 0.0f && hx < 1e30f && hy < 1e30f) {
+            ex = hx * 1.001f + 0.01f;
+            ey = hy * 1.001f + 0.01f;
+        } else {
+            ex = -1.0f;
+            ey = -1.0f;
+        }
+    } else {
+        if (!have_axes) cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, axes);
+        const float kx = (0.5f * W) / u.size[0];
+        const float ky = (0.5f * H) / u.size[1];
+        const float a00 = axes[0] * kx, a01 = axes[2] * kx;
+        const float a10 = -axes[1] * ky, a11 = -axes[3] * ky;
+        const float det = a00 * a11 - a01 * a10;
+        q0 = a11 / det;
+        q1 = -a01 / det;
+        q2 = -a10 / det;
+        q3 = a00 / det;
+        const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
+        const bool ok = det != 0.0f && isfinite(det) && isfinite(q0) && isfinite(q1) && isfinite(q2) &&
+                        isfinite(q3) && r2 >= 0.0f;
+        if (ok) {
+            ex = sqrtf(r2 * (a00 * a00 + a01 * a01)) * 1.001f + 0.01f;
+            ey = sqrtf(r2 * (a10 * a10 + a11 * a11)) * 1.001f + 0.01f;
+        } else {
+            ex = -1.0f;
+            ey = -1.0f;
+        }
+    }
+    float4 *sp = reinterpret_cast<float4 *>(P.splats + i);
+    sp[0] = make_float4(cx, cy, ex, ey);
+    sp[1] = make_float4(q0, q1, q2, q3);
+    sp[2] = make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f, rgba[3]);
+}
+
+// `pre` + `post` for an empty model: zero counts, no padding beyond capacity.
+__global__ void preprocess_empty_kernel(uint32_t *indirect, uint32_t *dispatch, Ctrl *ctrl) {
+    ctrl->count = 0;
+    if (indirect) {
+        indirect[0] = 6u;
+        indirect[1] = 0u;
+        indirect[2] = 0u;
+        indirect[3] = 0u;
+    }
+    if (dispatch) {
+        dispatch[0] = 0u;
+        dispatch[1] = 1u;
+        dispatch[2] = 1u;
+    }
+}
+
+size_t preprocess_scratch_bytes(uint32_t n) {
+    const size_t tiles = (n + kPreThreads - 1) / kPreThreads;
+    return align_up(sizeof(Ctrl), 256) + align_up(tiles * sizeof(uint64_t), 256);
+}
+
+cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, uint32_t format,
+                              uint32_t n, const uint32_t *selection, int invert, uint32_t *indirect,
+                              uint32_t *dispatch, uint32_t *indices, float *depths,
+                              uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st) {
+    Ctrl *ctrl = reinterpret_cast<Ctrl *>(scratch);
+    uint64_t *flags = reinterpret_cast<uint64_t *>((uint8_t *)scratch + align_up(sizeof(Ctrl), 256));
+    ctrl_init_kernel<<<1, 256, 0, st>>>(ctrl, 1);
+    count_launches(1);
+    if (n == 0) {
+        preprocess_empty_kernel<<<1, 1, 0, st>>>(indirect, dispatch, ctrl);
+        count_launches(1);
+        return cudaGetLastError();
+    }
+    PreParams P;
+    P.u = u;
+    P.records = reinterpret_cast<const uint8_t *>(records);
+    P.n = n;
+    P.ntiles = (n + kPreThreads - 1) / kPreThreads;
+    P.selection = selection;
+    P.invert = invert ? 1u : 0u;
+    P.indirect = indirect;
+    P.dispatch = dispatch;
+    P.indices = indices;
+    P.depths = depths;
+    P.depth_cap = depth_cap;
+    P.splats = splats;
+    P.ctrl = ctrl;
+    P.flags = flags;
+    prof_mark(kProfPreprocess, true, st);
+    count_launches(1);
+    switch (format) {
+        case GS_FORMAT_FP32:
+            preprocess_kernel<GS_FORMAT_FP32><<<P.ntiles, kPreThreads, 0, st>>>(P);
+            break;
+        case GS_FORMAT_HALF_SH_FP16:
+            preprocess_kernel<GS_FORMAT_HALF_SH_FP16><<<P.ntiles, kPreThreads, 0, st>>>(P);
+            break;
+        default:
+            preprocess_kernel<GS_FORMAT_HALF_SH_BF16><<<P.ntiles, kPreThreads, 0, st>>>(P);
+            break;
+    }
+    prof_mark(kProfPreprocess, false, st);
+    return cudaGetLastError();
+}
+
+}  // namespace gs
