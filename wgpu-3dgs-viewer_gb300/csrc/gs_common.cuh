@@ -75,6 +75,47 @@ __device__ __forceinline__ uint32_t look_back(const uint64_t *flags, uint32_t st
     return prefix;
 }
 
+// Warp-cooperative look-back of one counter (flags[j], j < tile), called by all 32 lanes of a
+// warp: each round reads 32 predecessors at once, adds every aggregate down to the nearest
+// inclusive prefix and stops there.  Returns the exclusive prefix in every lane.
+__device__ __forceinline__ uint32_t look_back_warp(const uint64_t *flags, uint32_t tile, uint32_t epoch,
+                                                   uint32_t *status) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t prefix = 0;
+    int64_t hi = (int64_t)tile;  // window is [hi - 32, hi)
+    uint32_t spins = 0;
+    while (hi > 0) {
+        const int64_t j = hi - 1 - (int64_t)lane;
+        uint64_t w;
+        if (j >= 0) {
+            w = ld_acquire(flags + j);
+        } else {
+            w = pack_flag(epoch, kFlagPrefix, 0u);  // before the first tile: an empty prefix
+        }
+        const bool ok = (uint32_t)(w >> 34) == epoch && ((uint32_t)(w >> 32) & 3u) != 0u;
+        const bool pre = ok && ((uint32_t)(w >> 32) & 3u) == kFlagPrefix;
+        const uint32_t pmask = __ballot_sync(0xFFFFFFFFu, pre);
+        const uint32_t bad = __ballot_sync(0xFFFFFFFFu, !ok);
+        const uint32_t upto = pmask ? (uint32_t)(__ffs(pmask) - 1) : 31u;  // lanes 0..upto needed
+        const uint32_t need = upto == 31u ? 0xFFFFFFFFu : ((2u << upto) - 1u);
+        if (bad & need) {
+            if (++spins > kSpinLimit) {
+                if (lane == 0) atomicOr(status, kStatusTimeout);
+                break;
+            }
+            if (spins > 64) __nanosleep(32);
+            continue;
+        }
+        uint32_t v = (lane <= upto) ? (uint32_t)w : 0u;
+#pragma unroll
+        for (uint32_t o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+        prefix += v;
+        if (pmask) break;
+        hi -= 32;
+    }
+    return prefix;
+}
+
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -104,6 +145,18 @@ __device__ __forceinline__ float exp_portable(float x) {
     p = fmaf(p, r, 1.0f);
     const int ki = (int)k;
     return __fmul_rn(p, __uint_as_float((uint32_t)(ki + 127) << 23));
+}
+
+// Fragment-bearing r² bound of a splat (see gs_splat.ex): a fragment with
+// alpha·exp(-r²) <= 1/512 cannot move an 8-bit channel; ln x <= ln2·(e + m - 1 + 0.0861).
+__device__ __forceinline__ float splat_r2_bound(float alpha, float std2) {
+    const float x = 512.0f * alpha;
+    if (!(x > 0.0f)) return -1.0f;
+    const uint32_t bits = __float_as_uint(x);
+    const float e = (float)((int)((bits >> 23) & 0xFFu) - 127);
+    const float mant = __uint_as_float((bits & 0x7FFFFFu) | 0x3F800000u);
+    const float r2 = 0.693147182f * (e + (mant - 1.0f) + 0.0862f) + 0.01f;
+    return (r2 < std2) ? r2 : std2;
 }
 
 // Scratch carving: 256-byte aligned sub-allocations.

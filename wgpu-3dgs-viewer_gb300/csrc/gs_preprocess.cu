@@ -267,18 +267,6 @@ __device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec
     rgba[3] = (float)((g.color >> 24) & 0xFFu) / 255.0f;
 }
 
-// Fragment-bearing r² bound of a splat (see gs_splat.ex): a fragment with
-// alpha·exp(-r²) <= 1/512 cannot move an 8-bit channel; ln x <= ln2·(e + m - 1 + 0.0861).
-__device__ __forceinline__ float splat_r2_bound(float alpha, float std2) {
-    const float x = 512.0f * alpha;
-    if (!(x > 0.0f)) return -1.0f;
-    const uint32_t bits = __float_as_uint(x);
-    const float e = (float)((int)((bits >> 23) & 0xFFu) - 127);
-    const float mant = __uint_as_float((bits & 0x7FFFFFu) | 0x3F800000u);
-    const float r2 = 0.693147182f * (e + (mant - 1.0f) + 0.0862f) + 0.01f;
-    return minf_wgsl(std2, r2);
-}
-
 // ---- mbarrier + bulk copy (global -> shared) ----------------------------------------------
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
@@ -379,7 +367,8 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
         }
     }
 
-    // ---- order-preserving compaction: ballot, block scan, decoupled look-back ----
+    // ---- order-preserving compaction: ballot + block scan; the CTA's count is published now
+    // and its global offset is looked up after the vertex work, which hides the wait ----
     const uint32_t bal = __ballot_sync(0xFFFFFFFFu, vis);
     if (lane == 0) s_warp[warp] = __popc(bal);
     __syncthreads();
@@ -390,30 +379,91 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
             s_warp[w] = run;
             run += c;
         }
-        const uint32_t total = run;
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            st_release(P.flags, pack_flag(epoch, kFlagPrefix, total));
-        } else {
-            st_release(P.flags + tile, pack_flag(epoch, kFlagAggregate, total));
-            prefix = look_back(P.flags, 1, tile, epoch, &P.ctrl->status);
-            st_release(P.flags + tile, pack_flag(epoch, kFlagPrefix, prefix + total));
-        }
-        s_base = prefix;
-        if (tile == P.ntiles - 1) {
-            // `post` (preprocess.wesl:108-126) and the DrawIndirectArgs instance count.
-            const uint32_t v = prefix + total;
-            P.ctrl->count = v;
-            if (P.indirect) {
-                P.indirect[0] = 6u;
-                P.indirect[1] = v;
-                P.indirect[2] = 0u;
-                P.indirect[3] = 0u;
+        s_base = run;  // block total until the look-back below
+        st_release(P.flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, run));
+    }
+
+    // ---- per-instance vertex work (render.wesl:75-130), written at the Gaussian's index ----
+    if (vis && P.splats) {
+        float rgba[4];
+        view_color<FMT>(u, g, world, rgba);
+        const float W = u.viewport[0], H = u.viewport[1];
+        const float cx = ((nx + 1.0f) * W) * 0.5f;
+        const float cy = ((1.0f - ny) * H) * 0.5f;
+        float q0, q1, q2, q3, ex, ey;
+        const float std2 = u.std_dev * u.std_dev;
+        const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
+        if (u.display_mode == GS_DISPLAY_POINT) {
+            float vp[4];
+            mat4_vec(u.vm, p4, vp);
+            const float l = sqrtf((vp[0] * vp[0] + vp[1] * vp[1]) + vp[2] * vp[2]);
+            const float aspect = u.size[1] / u.size[0];
+            const float pnd = (0.01f * u.point_size) / l;
+            const float hx = (pnd * aspect) * (0.5f * W);
+            const float hy = pnd * (0.5f * H);
+            q0 = hx;
+            q1 = hy;
+            q2 = 0.0f;
+            q3 = 0.0f;
+            if (hx > 0.0f && hy > 0.0f && hx < 1e30f && hy < 1e30f) {
+                ex = hx * 1.001f + 0.01f;
+                ey = hy * 1.001f + 0.01f;
+            } else {
+                ex = -1.0f;
+                ey = -1.0f;
             }
-            if (P.dispatch) {
-                P.dispatch[0] = (v + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS;
-                P.dispatch[1] = 1u;
-                P.dispatch[2] = 1u;
+        } else {
+            if (!have_axes) cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, axes);
+            const float kx = (0.5f * W) / u.size[0];
+            const float ky = (0.5f * H) / u.size[1];
+            const float a00 = axes[0] * kx, a01 = axes[2] * kx;
+            const float a10 = -axes[1] * ky, a11 = -axes[3] * ky;
+            const float det = a00 * a11 - a01 * a10;
+            q0 = a11 / det;
+            q1 = -a01 / det;
+            q2 = -a10 / det;
+            q3 = a00 / det;
+            const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
+            const bool ok = det != 0.0f && isfinite(det) && isfinite(q0) && isfinite(q1) && isfinite(q2) &&
+                            isfinite(q3) && r2 >= 0.0f;
+            if (ok) {
+                ex = sqrtf(r2 * (a00 * a00 + a01 * a01)) * 1.001f + 0.01f;
+                ey = sqrtf(r2 * (a10 * a10 + a11 * a11)) * 1.001f + 0.01f;
+            } else {
+                ex = -1.0f;
+                ey = -1.0f;
+            }
+        }
+        float4 *sp = reinterpret_cast<float4 *>(P.splats + i);
+        sp[0] = make_float4(cx, cy, ex, ey);
+        sp[1] = make_float4(q0, q1, q2, q3);
+        sp[2] = make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f,
+                            rgba[3]);
+    }
+
+    // ---- global offset: warp 0 looks back over the predecessors' published counts ----
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t total = s_base;
+        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(P.flags, tile, epoch, &P.ctrl->status);
+        if (lane == 0) {
+            if (tile > 0) st_release(P.flags + tile, pack_flag(epoch, kFlagPrefix, prefix + total));
+            s_base = prefix;
+            if (tile == P.ntiles - 1) {
+                // `post` (preprocess.wesl:108-126) and the DrawIndirectArgs instance count.
+                const uint32_t v = prefix + total;
+                P.ctrl->count = v;
+                if (P.indirect) {
+                    P.indirect[0] = 6u;
+                    P.indirect[1] = v;
+                    P.indirect[2] = 0u;
+                    P.indirect[3] = 0u;
+                }
+                if (P.dispatch) {
+                    P.dispatch[0] = (v + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS;
+                    P.dispatch[1] = 1u;
+                    P.dispatch[2] = 1u;
+                }
             }
         }
     }
@@ -423,66 +473,11 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
         const uint32_t padded = min(((v + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS) * GS_SORT_BLOCK_KVS, P.depth_cap);
         for (uint32_t k = v + tid; k < padded; k += kPreThreads) P.depths[k] = 2.0f;
     }
-    if (!vis) return;
-    const uint32_t c = s_base + s_warp[warp] + __popc(bal & lanemask_lt());
-    P.indices[c] = i;
-    P.depths[c] = key;
-    if (!P.splats) return;
-
-    // ---- per-instance vertex work (render.wesl:75-130) ----
-    float rgba[4];
-    view_color<FMT>(u, g, world, rgba);
-    const float W = u.viewport[0], H = u.viewport[1];
-    const float cx = ((nx + 1.0f) * W) * 0.5f;
-    const float cy = ((1.0f - ny) * H) * 0.5f;
-    float q0, q1, q2, q3, ex, ey;
-    const float std2 = u.std_dev * u.std_dev;
-    const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
-    if (u.display_mode == GS_DISPLAY_POINT) {
-        float vp[4];
-        mat4_vec(u.vm, p4, vp);
-        const float l = sqrtf((vp[0] * vp[0] + vp[1] * vp[1]) + vp[2] * vp[2]);
-        const float aspect = u.size[1] / u.size[0];
-        const float pnd = (0.01f * u.point_size) / l;
-        const float hx = (pnd * aspect) * (0.5f * W);
-        const float hy = pnd * (0.5f * H);
-        q0 = hx;
-        q1 = hy;
-        q2 = 0.0f;
-        q3 = 0.0f;
-        if (hx > 0.0f && hy > 0.0f && hx < 1e30f && hy < 1e30f) {
-            ex = hx * 1.001f + 0.01f;
-            ey = hy * 1.001f + 0.01f;
-        } else {
-            ex = -1.0f;
-            ey = -1.0f;
-        }
-    } else {
-        if (!have_axes) cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, axes);
-        const float kx = (0.5f * W) / u.size[0];
-        const float ky = (0.5f * H) / u.size[1];
-        const float a00 = axes[0] * kx, a01 = axes[2] * kx;
-        const float a10 = -axes[1] * ky, a11 = -axes[3] * ky;
-        const float det = a00 * a11 - a01 * a10;
-        q0 = a11 / det;
-        q1 = -a01 / det;
-        q2 = -a10 / det;
-        q3 = a00 / det;
-        const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
-        const bool ok = det != 0.0f && isfinite(det) && isfinite(q0) && isfinite(q1) && isfinite(q2) &&
-                        isfinite(q3) && r2 >= 0.0f;
-        if (ok) {
-            ex = sqrtf(r2 * (a00 * a00 + a01 * a01)) * 1.001f + 0.01f;
-            ey = sqrtf(r2 * (a10 * a10 + a11 * a11)) * 1.001f + 0.01f;
-        } else {
-            ex = -1.0f;
-            ey = -1.0f;
-        }
+    if (vis) {
+        const uint32_t c = s_base + s_warp[warp] + __popc(bal & lanemask_lt());
+        P.indices[c] = i;
+        P.depths[c] = key;
     }
-    float4 *sp = reinterpret_cast<float4 *>(P.splats + i);
-    sp[0] = make_float4(cx, cy, ex, ey);
-    sp[1] = make_float4(q0, q1, q2, q3);
-    sp[2] = make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f, rgba[3]);
 }
 
 // `pre` + `post` for an empty model: zero counts, no padding beyond capacity.

@@ -137,31 +137,34 @@ __global__ void __launch_bounds__(kBinThreads) bin_kernel(
     }
     if (lane == 31) s_tmp[warp] = x;
     __syncthreads();
-    if (tid == 0) {
-        uint32_t run = 0;
+    if (warp == 0) {
+        uint32_t run = 0, mine = 0;
         for (uint32_t i = 0; i < kBinThreads / 32; ++i) {
             const uint32_t c = s_tmp[i];
-            s_tmp[i] = run;
+            if (lane == i) mine = run;
             run += c;
         }
         const uint32_t total = run;
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            st_release(flags, pack_flag(epoch, kFlagPrefix, total));
-        } else {
-            st_release(flags + tile, pack_flag(epoch, kFlagAggregate, total));
-            prefix = look_back(flags, 1, tile, epoch, &ctrl->status);
-            const uint64_t incl = (uint64_t)prefix + total;
-            st_release(flags + tile, pack_flag(epoch, kFlagPrefix, incl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)incl));
-        }
-        s_base = prefix;
-        if (tile == ntiles - 1) {
-            const uint64_t want = (uint64_t)s_seg_want + prefix + total;
-            const uint32_t kept = want > max_pairs ? max_pairs : (uint32_t)want;
-            if (want > max_pairs) atomicOr(&ctrl->status, kStatusCapacity);
-            ctrl->total = want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want;
-            ctrl->count = kept;
-            ctrl->pair_base = kept;
+        if (lane == 0)
+            st_release(flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, total));
+        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(flags, tile, epoch, &ctrl->status);
+        __syncwarp();
+        if (lane < kBinThreads / 32) s_tmp[lane] = mine;
+        if (lane == 0) {
+            if (tile > 0) {
+                const uint64_t incl = (uint64_t)prefix + total;
+                st_release(flags + tile,
+                           pack_flag(epoch, kFlagPrefix, incl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)incl));
+            }
+            s_base = prefix;
+            if (tile == ntiles - 1) {
+                const uint64_t want = (uint64_t)s_seg_want + prefix + total;
+                const uint32_t kept = want > max_pairs ? max_pairs : (uint32_t)want;
+                if (want > max_pairs) atomicOr(&ctrl->status, kStatusCapacity);
+                ctrl->total = want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want;
+                ctrl->count = kept;
+                ctrl->pair_base = kept;
+            }
         }
     }
     __syncthreads();
@@ -213,17 +216,21 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
     const gs_splat *__restrict__ sorted, const uint32_t *__restrict__ pair_val, const uint2 *__restrict__ ranges,
     uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch, uint32_t tiles_x, float std2,
     float outline2, uint32_t max_splats) {
+    // Staged chunk of the tile's splats: a = (cx, cy, r² limit, alpha), b = q (or point half
+    // sides), c = (s255.rgb, -), box = fragment box in pixel-centre coordinates.
     __shared__ float4 s_a[kRasterThreads], s_b[kRasterThreads], s_c[kRasterThreads];
     __shared__ float4 s_box[kRasterThreads];
+    // Per-warp list of chunk entries whose box meets the warp's 8x4 pixel block, in draw order.
+    __shared__ uint8_t s_list[kRasterThreads / 32][kRasterThreads];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
     const uint2 range = ranges[blockIdx.x];
-    // Each warp owns an 8x4 block of the 16x16 tile.
     const uint32_t wx0 = tx * GS_TILE + (warp & 1u) * 8u, wy0 = ty * GS_TILE + (warp >> 1) * 4u;
     const uint32_t px = wx0 + (lane & 7u), py = wy0 + (lane >> 3);
     const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
     const float bx0 = (float)wx0 + 0.5f, bx1 = (float)wx0 + 7.5f;
     const float by0 = (float)wy0 + 0.5f, by1 = (float)wy0 + 3.5f;
+    const uint32_t lt = lanemask_lt();
     float dr = 0.0f, dg = 0.0f, db = 0.0f;
 
     for (uint32_t base = range.x; base < range.y; base += kRasterThreads) {
@@ -237,18 +244,32 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
                 b = __ldg(src + 1);
                 c = __ldg(src + 2);
             }
-            s_a[tid] = a;
+            // Fragments beyond the r² limit cannot change the pixel (see splat_r2_bound).
+            const float lim = (MODE == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, std2) : std2;
+            s_a[tid] = make_float4(a.x, a.y, lim, c.w);
             s_b[tid] = b;
             s_c[tid] = c;
             s_box[tid] = make_float4(a.x - a.z, a.x + a.z, a.y - a.w, a.y + a.w);
         }
         __syncthreads();
-        for (uint32_t j = 0; j < cnt; ++j) {
-            const float4 box = s_box[j];
-            if (box.y < bx0 || box.x > bx1 || box.w < by0 || box.z > by1) continue;  // warp-uniform
+        uint32_t nl = 0;
+        for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
+            const uint32_t j = j0 + lane;
+            bool hit = false;
+            if (j < cnt) {
+                const float4 box = s_box[j];
+                hit = !(box.y < bx0 || box.x > bx1 || box.w < by0 || box.z > by1);
+            }
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
+            if (hit) s_list[warp][nl + __popc(m & lt)] = (uint8_t)j;
+            nl += __popc(m);
+        }
+        __syncwarp();
+        for (uint32_t i = 0; i < nl; ++i) {
+            const uint32_t j = s_list[warp][i];
             const float4 a = s_a[j];
-            const float dx = __fsub_rn(pxc, a.x), dy = __fsub_rn(pyc, a.y);
             const float4 b = s_b[j];
+            const float dx = __fsub_rn(pxc, a.x), dy = __fsub_rn(pyc, a.y);
             float alpha;
             if constexpr (MODE == GS_DISPLAY_POINT) {
                 if (!(dx >= -b.x && dx < b.x && dy >= -b.y && dy < b.y)) continue;
@@ -257,12 +278,12 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
                 const float qx = fmaf(b.x, dx, __fmul_rn(b.y, dy));
                 const float qy = fmaf(b.z, dx, __fmul_rn(b.w, dy));
                 const float r2 = fmaf(qx, qx, __fmul_rn(qy, qy));
-                if (!(r2 <= std2)) continue;
+                if (!(r2 <= a.z)) continue;
                 if constexpr (MODE == GS_DISPLAY_SPLAT) {
                     const float e = PORTABLE_EXP ? exp_portable(-r2) : __expf(-r2);
-                    alpha = __fmul_rn(s_c[j].w, e);
+                    alpha = __fmul_rn(a.w, e);
                 } else {
-                    alpha = (r2 > outline2) ? 1.0f : s_c[j].w;
+                    alpha = (r2 > outline2) ? 1.0f : a.w;
                 }
             }
             const float4 c = s_c[j];

@@ -42,8 +42,10 @@ __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t m
     return count ? min(*count, max_count) : max_count;
 }
 
-// Global digit histograms of all passes in one read of the keys.  Warp-aggregated shared
-// atomics keep the nearly constant high digits of float depth keys from serialising.
+// Global digit histograms of all passes in one read of the keys.  Per pass, the warp counts
+// the digit of lane 0 with one ballot (the high digits of float depth keys are nearly
+// constant, and same-address shared atomics would serialise) and the other keys with plain
+// shared atomics.
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restrict__ keys,
                                                         const uint32_t *count, uint32_t max_count,
                                                         uint32_t npasses, Ctrl *ctrl) {
@@ -53,16 +55,17 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
     const uint32_t n = load_count(count, max_count);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31u;
-    // Every lane of a warp runs the same number of iterations (bounds padded to the warp),
-    // so the match below always sees a full warp.
+    // Whole warps iterate together (bounds padded to the warp) so the ballots see 32 lanes.
     const uint32_t nr = (n + 31u) & ~31u;
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nr; idx += stride) {
         const bool valid = idx < n;
         const uint32_t k = valid ? keys[idx] : 0u;
         for (uint32_t p = 0; p < npasses; ++p) {
-            const uint32_t d = valid ? ((k >> (8u * p)) & 255u) : 256u + lane;
-            const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-            if (valid && (__ffs(peers) - 1) == (int)lane) atomicAdd(&h[p][d], (uint32_t)__popc(peers));
+            const uint32_t d = (k >> (8u * p)) & 255u;
+            const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+            const uint32_t same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
+            if (lane == 0 && same) atomicAdd(&h[p][d0], (uint32_t)__popc(same));
+            if (valid && d != d0) atomicAdd(&h[p][d], 1u);
         }
     }
     __syncthreads();
