@@ -86,3 +86,19 @@ def test_repeated_frames_identical(gs, cuda):
     a = pipe.render(u)
     for _ in range(3):
         assert np.array_equal(pipe.render(u), a)
+
+
+@pytest.mark.parametrize("suffix_min,eps", [("0", "1e-5"), ("0", "0.5"), ("0", "1e-30"), ("1000000000", "1e-5")])
+@pytest.mark.parametrize("mode", MODES)
+def test_early_out_paths_bit_exact(gs, cuda, oracle, monkeypatch, suffix_min, eps, mode):
+    """The single pass and the early-out (with many or no restarts) give the oracle's frame."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    monkeypatch.setenv("GS300_SUFFIX_MIN", suffix_min)
+    monkeypatch.setenv("GS300_SUFFIX_EPS", eps)
+    n, w, h = 60_000, 256, 160
+    sc = S.synth_scene(n, seed=25)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, w, h)
+    u = uniforms(gs, w, h, k=12, mode=mode, radius=6.0)
+    got = pipe.render(u)
+    want = _oracle_frame(oracle, u, sc, R.FORMAT_FP32, w, h, exp_mode=0, threads=8)
+    assert np.array_equal(got, want), f"{(got != want).any(axis=-1).sum()} pixels differ"

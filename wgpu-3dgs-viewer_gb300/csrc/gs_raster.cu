@@ -15,6 +15,8 @@
 //     every fragment: d' = round(d·(1-α) + s·α) in units of 1/255.
 // Fragments whose alpha cannot move an 8-bit channel (alpha <= 1/512) lie outside the splat's
 // fragment box and are never visited; skipping them leaves every pixel bit-identical.
+#include <cstdlib>
+
 #include "gs_internal.h"
 
 namespace gs {
@@ -73,6 +75,21 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_
 }
 
 const Ctrl *raster_ctrl(const void *scratch) { return reinterpret_cast<const Ctrl *>(scratch); }
+
+// Early-out knobs of the rasteriser (results are identical for any values): tiles with fewer
+// list entries than `suffix_min` take the single pass; `eps` is the transmittance that ends the
+// front-to-back walk.  Overridable for tuning by GS300_SUFFIX_MIN / GS300_SUFFIX_EPS.
+struct RasterTuning {
+    uint32_t suffix_min;
+    float eps;
+};
+
+static RasterTuning raster_tuning() {
+    RasterTuning r{2048u, 1e-6f};
+    if (const char *v = getenv("GS300_SUFFIX_MIN")) r.suffix_min = (uint32_t)strtoul(v, nullptr, 10);
+    if (const char *v = getenv("GS300_SUFFIX_EPS")) r.eps = strtof(v, nullptr);
+    return r;
+}
 
 // Tile rectangle of a splat's fragment box; false when it touches no tile.
 __device__ __forceinline__ bool tile_rect(const float4 a, uint32_t tiles_x, uint32_t tiles_y, uint32_t *x0,
@@ -211,91 +228,215 @@ __global__ void tile_ranges_kernel(const uint32_t *__restrict__ key, const Ctrl 
 // The tile sort keeps its own control block; fold its status bits into the raster's.
 __global__ void merge_status_kernel(Ctrl *dst, const Ctrl *src) { dst->status |= src->status; }
 
+// One fragment of a staged splat at the pixel centre (pxc, pyc) (render.wesl:143-181):
+// false when discarded or when it cannot change the pixel, else its alpha.
+template <uint32_t MODE, bool PORTABLE_EXP>
+__device__ __forceinline__ bool fragment(const float4 a, const float4 b, float pxc, float pyc, float outline2,
+                                         float *alpha) {
+    const float dx = __fsub_rn(pxc, a.x), dy = __fsub_rn(pyc, a.y);
+    if constexpr (MODE == GS_DISPLAY_POINT) {
+        if (!(dx >= -b.x && dx < b.x && dy >= -b.y && dy < b.y)) return false;
+        *alpha = 1.0f;
+        return true;
+    } else {
+        const float qx = fmaf(b.x, dx, __fmul_rn(b.y, dy));
+        const float qy = fmaf(b.z, dx, __fmul_rn(b.w, dy));
+        const float r2 = fmaf(qx, qx, __fmul_rn(qy, qy));
+        if (!(r2 <= a.z)) return false;
+        if constexpr (MODE == GS_DISPLAY_SPLAT) {
+            const float e = PORTABLE_EXP ? exp_portable(-r2) : __expf(-r2);
+            *alpha = __fmul_rn(a.w, e);
+        } else {
+            *alpha = (r2 > outline2) ? 1.0f : a.w;
+        }
+        return true;
+    }
+}
+
+// BlendState::ALPHA_BLENDING onto an 8-bit channel, in units of 1/255: round(d·(1-α) + s·α).
+__device__ __forceinline__ float blend8(float d, float om, float s_alpha) { return rint_small(fmaf(d, om, s_alpha)); }
+
+struct RasterShared {
+    float4 a[kRasterThreads];    // cx, cy, r² limit, alpha
+    float4 b[kRasterThreads];    // q (or the point half sides)
+    float4 c[kRasterThreads];    // s255.rgb
+    float4 box[kRasterThreads];  // fragment box in pixel-centre coordinates
+    uint8_t list[kRasterThreads / 32][kRasterThreads];
+    uint32_t kmin;
+};
+
+// Stage list entries [rel0, rel0 + cnt) of the tile (cnt <= 256), one per thread.
+template <uint32_t MODE>
+__device__ __forceinline__ void stage_chunk(RasterShared &S, const gs_splat *__restrict__ sorted,
+                                            const uint32_t *__restrict__ pair_val, uint32_t first, uint32_t cnt,
+                                            float std2, uint32_t max_splats) {
+    const uint32_t tid = threadIdx.x;
+    if (tid < cnt) {
+        const uint32_t k = pair_val[first + tid];
+        float4 a = make_float4(0.0f, 0.0f, -1.0f, -1.0f), b = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = b;
+        if (k < max_splats) {  // ranks come from the tile sort; false only after a timeout
+            const float4 *src = reinterpret_cast<const float4 *>(sorted + k);
+            a = __ldg(src);
+            b = __ldg(src + 1);
+            c = __ldg(src + 2);
+        }
+        // Fragments beyond the r² limit cannot change the pixel (see splat_r2_bound).
+        const float lim = (MODE == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, std2) : std2;
+        S.a[tid] = make_float4(a.x, a.y, lim, c.w);
+        S.b[tid] = b;
+        S.c[tid] = c;
+        S.box[tid] = make_float4(a.x - a.z, a.x + a.z, a.y - a.w, a.y + a.w);
+    }
+}
+
+// The calling warp's list of staged entries whose box meets its pixel block, in draw order.
+__device__ __forceinline__ uint32_t compact_chunk(RasterShared &S, uint32_t cnt, float bx0, float bx1, float by0,
+                                                  float by1) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t lt = lanemask_lt();
+    uint32_t nl = 0;
+    for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
+        const uint32_t j = j0 + lane;
+        bool hit = false;
+        if (j < cnt) {
+            const float4 box = S.box[j];
+            hit = !(box.y < bx0 || box.x > bx1 || box.w < by0 || box.z > by1);
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
+        if (hit) S.list[warp][nl + __popc(m & lt)] = (uint8_t)j;
+        nl += __popc(m);
+    }
+    __syncwarp();
+    return nl;
+}
+
+// K4.  One CTA per 16x16 tile; each warp owns an 8x4 pixel block, each thread one pixel.
+// Short tile lists are blended back to front in one pass.  Long ones use an exact early-out:
+//   A. walk the list front to back (nearest first) until the pixel's transmittance drops
+//      below `eps`, at list position k;
+//   B. blend positions k.. back to front twice, from destination 0 and from 255.  The blend
+//      with 8-bit rounding is monotone in the destination, so the two results bound the
+//      result of every history before k; when they meet, that is the exact pixel.  A pixel
+//      whose bounds do not meet restarts B from k - (n - k) (k = 0 starts from the cleared
+//      value, which is exact).
+// Every pixel therefore ends bit-identical to the full back-to-front pass.
 template <uint32_t MODE, bool PORTABLE_EXP>
 __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
     const gs_splat *__restrict__ sorted, const uint32_t *__restrict__ pair_val, const uint2 *__restrict__ ranges,
     uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch, uint32_t tiles_x, float std2,
-    float outline2, uint32_t max_splats) {
-    // Staged chunk of the tile's splats: a = (cx, cy, r² limit, alpha), b = q (or point half
-    // sides), c = (s255.rgb, -), box = fragment box in pixel-centre coordinates.
-    __shared__ float4 s_a[kRasterThreads], s_b[kRasterThreads], s_c[kRasterThreads];
-    __shared__ float4 s_box[kRasterThreads];
-    // Per-warp list of chunk entries whose box meets the warp's 8x4 pixel block, in draw order.
-    __shared__ uint8_t s_list[kRasterThreads / 32][kRasterThreads];
+    float outline2, uint32_t max_splats, uint32_t suffix_min, float eps) {
+    __shared__ RasterShared S;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
     const uint2 range = ranges[blockIdx.x];
+    const uint32_t s0 = range.x, n = range.y - range.x;
     const uint32_t wx0 = tx * GS_TILE + (warp & 1u) * 8u, wy0 = ty * GS_TILE + (warp >> 1) * 4u;
     const uint32_t px = wx0 + (lane & 7u), py = wy0 + (lane >> 3);
     const float pxc = (float)px + 0.5f, pyc = (float)py + 0.5f;
     const float bx0 = (float)wx0 + 0.5f, bx1 = (float)wx0 + 7.5f;
     const float by0 = (float)wy0 + 0.5f, by1 = (float)wy0 + 3.5f;
-    const uint32_t lt = lanemask_lt();
-    float dr = 0.0f, dg = 0.0f, db = 0.0f;
+    float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f;
 
-    for (uint32_t base = range.x; base < range.y; base += kRasterThreads) {
-        const uint32_t cnt = min(kRasterThreads, range.y - base);
-        if (tid < cnt) {
-            const uint32_t k = pair_val[base + tid];
-            float4 a = make_float4(0.0f, 0.0f, -1.0f, -1.0f), b = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = b;
-            if (k < max_splats) {  // ranks come from the tile sort; false only after a timeout
-                const float4 *src = reinterpret_cast<const float4 *>(sorted + k);
-                a = __ldg(src);
-                b = __ldg(src + 1);
-                c = __ldg(src + 2);
+    if (n < suffix_min) {
+        for (uint32_t base = 0; base < n; base += kRasterThreads) {
+            const uint32_t cnt = min(kRasterThreads, n - base);
+            stage_chunk<MODE>(S, sorted, pair_val, s0 + base, cnt, std2, max_splats);
+            __syncthreads();
+            const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
+            for (uint32_t i = 0; i < nl; ++i) {
+                const uint32_t j = S.list[warp][i];
+                float al;
+                if (!fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) continue;
+                const float4 c = S.c[j];
+                const float om = __fsub_rn(1.0f, al);
+                d0 = blend8(d0, om, __fmul_rn(c.x, al));
+                d1 = blend8(d1, om, __fmul_rn(c.y, al));
+                d2 = blend8(d2, om, __fmul_rn(c.z, al));
             }
-            // Fragments beyond the r² limit cannot change the pixel (see splat_r2_bound).
-            const float lim = (MODE == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, std2) : std2;
-            s_a[tid] = make_float4(a.x, a.y, lim, c.w);
-            s_b[tid] = b;
-            s_c[tid] = c;
-            s_box[tid] = make_float4(a.x - a.z, a.x + a.z, a.y - a.w, a.y + a.w);
+            __syncthreads();
         }
-        __syncthreads();
-        uint32_t nl = 0;
-        for (uint32_t j0 = 0; j0 < cnt; j0 += 32) {
-            const uint32_t j = j0 + lane;
-            bool hit = false;
-            if (j < cnt) {
-                const float4 box = s_box[j];
-                hit = !(box.y < bx0 || box.x > bx1 || box.w < by0 || box.z > by1);
-            }
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
-            if (hit) s_list[warp][nl + __popc(m & lt)] = (uint8_t)j;
-            nl += __popc(m);
-        }
-        __syncwarp();
-        for (uint32_t i = 0; i < nl; ++i) {
-            const uint32_t j = s_list[warp][i];
-            const float4 a = s_a[j];
-            const float4 b = s_b[j];
-            const float dx = __fsub_rn(pxc, a.x), dy = __fsub_rn(pyc, a.y);
-            float alpha;
-            if constexpr (MODE == GS_DISPLAY_POINT) {
-                if (!(dx >= -b.x && dx < b.x && dy >= -b.y && dy < b.y)) continue;
-                alpha = 1.0f;
-            } else {
-                const float qx = fmaf(b.x, dx, __fmul_rn(b.y, dy));
-                const float qy = fmaf(b.z, dx, __fmul_rn(b.w, dy));
-                const float r2 = fmaf(qx, qx, __fmul_rn(qy, qy));
-                if (!(r2 <= a.z)) continue;
-                if constexpr (MODE == GS_DISPLAY_SPLAT) {
-                    const float e = PORTABLE_EXP ? exp_portable(-r2) : __expf(-r2);
-                    alpha = __fmul_rn(a.w, e);
-                } else {
-                    alpha = (r2 > outline2) ? 1.0f : a.w;
+    } else {
+        // ---- A: front-to-back transmittance to find the start position k ----
+        float T = 1.0f;
+        uint32_t k = 0;
+        bool found = false;
+        for (uint32_t end = n; end > 0;) {
+            const uint32_t base = end > kRasterThreads ? end - kRasterThreads : 0u;
+            const uint32_t cnt = end - base;
+            stage_chunk<MODE>(S, sorted, pair_val, s0 + base, cnt, std2, max_splats);
+            __syncthreads();
+            if (__any_sync(0xFFFFFFFFu, !found)) {
+                const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
+                for (int i = (int)nl - 1; i >= 0; --i) {
+                    if (__all_sync(0xFFFFFFFFu, found)) break;
+                    const uint32_t j = S.list[warp][i];
+                    float al;
+                    if (!found && fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) {
+                        T = __fmul_rn(T, __fsub_rn(1.0f, al));
+                        if (T < eps) {
+                            found = true;
+                            k = base + j;
+                        }
+                    }
                 }
             }
-            const float4 c = s_c[j];
-            const float om = __fsub_rn(1.0f, alpha);
-            dr = rint_small(fmaf(dr, om, __fmul_rn(c.x, alpha)));
-            dg = rint_small(fmaf(dg, om, __fmul_rn(c.y, alpha)));
-            db = rint_small(fmaf(db, om, __fmul_rn(c.z, alpha)));
+            if (__syncthreads_and(found)) break;
+            end = base;
         }
-        __syncthreads();
+        if (!found) k = 0;
+        // ---- B: bounded back-to-front passes from k ----
+        bool active = true;
+        float h0 = 0.0f, h1 = 0.0f, h2 = 0.0f;
+        for (;;) {
+            if (tid == 0) S.kmin = 0xFFFFFFFFu;
+            __syncthreads();
+            const uint32_t wmin = __reduce_min_sync(0xFFFFFFFFu, active ? k : 0xFFFFFFFFu);
+            if (lane == 0 && wmin != 0xFFFFFFFFu) atomicMin(&S.kmin, wmin);
+            __syncthreads();
+            const uint32_t kmin = S.kmin;
+            if (kmin == 0xFFFFFFFFu) break;
+            if (active) {
+                const float top = (k == 0) ? 0.0f : 255.0f;
+                d0 = d1 = d2 = 0.0f;
+                h0 = h1 = h2 = top;
+            }
+            for (uint32_t base = kmin / kRasterThreads * kRasterThreads; base < n; base += kRasterThreads) {
+                const uint32_t cnt = min(kRasterThreads, n - base);
+                __syncthreads();
+                stage_chunk<MODE>(S, sorted, pair_val, s0 + base, cnt, std2, max_splats);
+                __syncthreads();
+                if (__any_sync(0xFFFFFFFFu, active)) {
+                    const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
+                    for (uint32_t i = 0; i < nl; ++i) {
+                        const uint32_t j = S.list[warp][i];
+                        float al;
+                        if (!active || base + j < k) continue;
+                        if (!fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) continue;
+                        const float4 c = S.c[j];
+                        const float om = __fsub_rn(1.0f, al);
+                        const float s0a = __fmul_rn(c.x, al), s1a = __fmul_rn(c.y, al), s2a = __fmul_rn(c.z, al);
+                        d0 = blend8(d0, om, s0a);
+                        d1 = blend8(d1, om, s1a);
+                        d2 = blend8(d2, om, s2a);
+                        h0 = blend8(h0, om, s0a);
+                        h1 = blend8(h1, om, s1a);
+                        h2 = blend8(h2, om, s2a);
+                    }
+                }
+            }
+            __syncthreads();
+            if (active) {
+                if (d0 == h0 && d1 == h1 && d2 == h2) {
+                    active = false;
+                } else {
+                    const uint32_t suffix = n - k;
+                    k = k > suffix ? k - suffix : 0u;
+                }
+            }
+        }
     }
     if (px < W && py < H) {
-        const uint32_t rgba = (uint32_t)dr | ((uint32_t)dg << 8) | ((uint32_t)db << 16) | 0xFF000000u;
+        const uint32_t rgba = (uint32_t)d0 | ((uint32_t)d1 << 8) | ((uint32_t)d2 << 16) | 0xFF000000u;
         *reinterpret_cast<uint32_t *>(target + (size_t)py * pitch + (size_t)px * 4u) = rgba;
     }
 }
@@ -303,12 +444,13 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
 template <uint32_t MODE>
 static void launch_raster_mode(const RasterLayout &L, uint8_t *target, uint32_t W, uint32_t H, uint32_t pitch,
                                float std2, float outline2, int exact, uint32_t max_splats, cudaStream_t st) {
+    const RasterTuning t = raster_tuning();
     if (exact)
-        raster_kernel<MODE, true><<<L.ntiles, kRasterThreads, 0, st>>>(L.sorted, L.pair_val, L.ranges, target, W, H,
-                                                                       pitch, L.tiles_x, std2, outline2, max_splats);
+        raster_kernel<MODE, true><<<L.ntiles, kRasterThreads, 0, st>>>(
+            L.sorted, L.pair_val, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
     else
-        raster_kernel<MODE, false><<<L.ntiles, kRasterThreads, 0, st>>>(L.sorted, L.pair_val, L.ranges, target, W,
-                                                                        H, pitch, L.tiles_x, std2, outline2, max_splats);
+        raster_kernel<MODE, false><<<L.ntiles, kRasterThreads, 0, st>>>(
+            L.sorted, L.pair_val, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
 }
 
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
