@@ -33,6 +33,14 @@ size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits);
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage = kProfDepthSort);
 
+// Packed (uint2 {key, value}) in-place sort for internal pair lists whose digit histograms
+// the producer accumulated into the control block after sort_pairs_begin().
+size_t sort_pairs_scratch_bytes(uint32_t max_count, uint32_t key_bits);
+Ctrl *sort_pairs_ctrl(void *scratch);
+cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st);
+cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits,
+                              void *scratch, cudaStream_t st);
+
 // ---- K3 binning + K4 raster (gs_raster.cu) ----
 struct RasterSegment {
     const gs_splat *splats;       // indexed by Gaussian index

@@ -28,8 +28,7 @@ struct RasterLayout {
     Ctrl *ctrl;
     gs_splat *sorted;    // draw-ordered splats, capacity max_splats
     uint64_t *flags;     // bin look-back flags, ceil(max_splats / 256)
-    uint32_t *pair_key;  // capacity max_pairs
-    uint32_t *pair_val;
+    uint2 *pairs;        // (tile, draw rank), capacity max_pairs
     uint2 *ranges;       // per tile [start, end)
     void *sort_scratch;
     uint32_t tiles_x, tiles_y, ntiles, key_bits;
@@ -55,10 +54,8 @@ static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w
     p += align_up((size_t)max_splats * sizeof(gs_splat), 256);
     L.flags = reinterpret_cast<uint64_t *>(p);
     p += align_up(((size_t)max_splats + kBinThreads - 1) / kBinThreads * 8 + 8, 256);
-    L.pair_key = reinterpret_cast<uint32_t *>(p);
-    p += align_up((size_t)max_pairs * 4, 256);
-    L.pair_val = reinterpret_cast<uint32_t *>(p);
-    p += align_up((size_t)max_pairs * 4, 256);
+    L.pairs = reinterpret_cast<uint2 *>(p);
+    p += align_up((size_t)max_pairs * 8, 256);
     L.ranges = reinterpret_cast<uint2 *>(p);
     p += align_up((size_t)L.ntiles * sizeof(uint2), 256);
     L.sort_scratch = p;
@@ -70,8 +67,8 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_
     const uint32_t key_bits = bits_for(tiles > 0 ? tiles - 1 : 0);
     return align_up(sizeof(Ctrl), 256) + align_up((size_t)max_splats * sizeof(gs_splat), 256) +
            align_up(((size_t)max_splats + kBinThreads - 1) / kBinThreads * 8 + 8, 256) +
-           2 * align_up((size_t)max_pairs * 4, 256) + align_up((size_t)tiles * sizeof(uint2), 256) +
-           sort_scratch_bytes(max_pairs, key_bits);
+           align_up((size_t)max_pairs * 8, 256) + align_up((size_t)tiles * sizeof(uint2), 256) +
+           sort_pairs_scratch_bytes(max_pairs, key_bits);
 }
 
 const Ctrl *raster_ctrl(const void *scratch) { return reinterpret_cast<const Ctrl *>(scratch); }
@@ -113,14 +110,16 @@ __device__ __forceinline__ bool tile_rect(const float4 a, uint32_t tiles_x, uint
 // K3: gather into draw order + count tiles + scan + emit (tile, rank) pairs.
 __global__ void __launch_bounds__(kBinThreads) bin_kernel(
     const gs_splat *__restrict__ splats, const uint32_t *__restrict__ sorted_index, const uint32_t *count,
-    uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, uint32_t *__restrict__ pair_key,
-    uint32_t *__restrict__ pair_val, uint32_t max_pairs, uint32_t tiles_x, uint32_t tiles_y, Ctrl *ctrl,
-    uint64_t *flags) {
+    uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, uint2 *__restrict__ pairs,
+    uint32_t max_pairs, uint32_t tiles_x, uint32_t tiles_y, Ctrl *ctrl, uint64_t *flags, Ctrl *sort_ctrl,
+    uint32_t key_passes) {
     __shared__ uint32_t s_incl[kBinThreads];
     __shared__ uint32_t s_x0[kBinThreads], s_y0[kBinThreads], s_w[kBinThreads];
     __shared__ uint32_t s_tmp[kBinThreads / 32];
     __shared__ uint32_t s_tile, s_epoch, s_base, s_seg_base, s_seg_want;
+    __shared__ uint32_t s_hist[4][256];  // digit histograms of the emitted tile ids (tile sort)
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    for (uint32_t i = tid; i < 4 * 256; i += kBinThreads) (&s_hist[0][0])[i] = 0u;
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
         s_seg_base = *(volatile uint32_t *)&ctrl->pair_base;
@@ -208,20 +207,26 @@ __global__ void __launch_bounds__(kBinThreads) bin_kernel(
         const uint32_t tyy = s_y0[owner] + r / ww, txx = s_x0[owner] + r % ww;
         const uint64_t o = out0 + j;
         if (o < max_pairs) {
-            pair_key[o] = tyy * tiles_x + txx;
-            pair_val[o] = rank_offset + tile * kBinThreads + owner;
+            const uint32_t t = tyy * tiles_x + txx;
+            pairs[o] = make_uint2(t, rank_offset + tile * kBinThreads + owner);
+            for (uint32_t p = 0; p < key_passes; ++p) atomicAdd(&s_hist[p][(t >> (8u * p)) & 255u], 1u);
         }
+    }
+    __syncthreads();
+    for (uint32_t p = 0; p < key_passes; ++p) {
+        const uint32_t v = s_hist[p][tid];
+        if (v) atomicAdd(&sort_ctrl->hist[p][tid], v);
     }
 }
 
-__global__ void tile_ranges_kernel(const uint32_t *__restrict__ key, const Ctrl *ctrl, uint2 *ranges,
+__global__ void tile_ranges_kernel(const uint2 *__restrict__ pairs, const Ctrl *ctrl, uint2 *ranges,
                                    uint32_t ntiles) {
     const uint32_t n = ctrl->count;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint32_t t = key[p];
+        const uint32_t t = pairs[p].x;
         if (t >= ntiles) continue;
-        if (p == 0 || key[p - 1] != t) ranges[t].x = p;
-        if (p == n - 1 || key[p + 1] != t) ranges[t].y = p + 1;
+        if (p == 0 || pairs[p - 1].x != t) ranges[t].x = p;
+        if (p == n - 1 || pairs[p + 1].x != t) ranges[t].y = p + 1;
     }
 }
 
@@ -268,11 +273,11 @@ struct RasterShared {
 // Stage list entries [rel0, rel0 + cnt) of the tile (cnt <= 256), one per thread.
 template <uint32_t MODE>
 __device__ __forceinline__ void stage_chunk(RasterShared &S, const gs_splat *__restrict__ sorted,
-                                            const uint32_t *__restrict__ pair_val, uint32_t first, uint32_t cnt,
+                                            const uint2 *__restrict__ pairs, uint32_t first, uint32_t cnt,
                                             float std2, uint32_t max_splats) {
     const uint32_t tid = threadIdx.x;
     if (tid < cnt) {
-        const uint32_t k = pair_val[first + tid];
+        const uint32_t k = pairs[first + tid].y;
         float4 a = make_float4(0.0f, 0.0f, -1.0f, -1.0f), b = make_float4(0.0f, 0.0f, 0.0f, 0.0f), c = b;
         if (k < max_splats) {  // ranks come from the tile sort; false only after a timeout
             const float4 *src = reinterpret_cast<const float4 *>(sorted + k);
@@ -322,7 +327,7 @@ __device__ __forceinline__ uint32_t compact_chunk(RasterShared &S, uint32_t cnt,
 // Every pixel therefore ends bit-identical to the full back-to-front pass.
 template <uint32_t MODE, bool PORTABLE_EXP>
 __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
-    const gs_splat *__restrict__ sorted, const uint32_t *__restrict__ pair_val, const uint2 *__restrict__ ranges,
+    const gs_splat *__restrict__ sorted, const uint2 *__restrict__ pairs, const uint2 *__restrict__ ranges,
     uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch, uint32_t tiles_x, float std2,
     float outline2, uint32_t max_splats, uint32_t suffix_min, float eps) {
     __shared__ RasterShared S;
@@ -340,7 +345,7 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
     if (n < suffix_min) {
         for (uint32_t base = 0; base < n; base += kRasterThreads) {
             const uint32_t cnt = min(kRasterThreads, n - base);
-            stage_chunk<MODE>(S, sorted, pair_val, s0 + base, cnt, std2, max_splats);
+            stage_chunk<MODE>(S, sorted, pairs, s0 + base, cnt, std2, max_splats);
             __syncthreads();
             const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
             for (uint32_t i = 0; i < nl; ++i) {
@@ -363,7 +368,7 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
         for (uint32_t end = n; end > 0;) {
             const uint32_t base = end > kRasterThreads ? end - kRasterThreads : 0u;
             const uint32_t cnt = end - base;
-            stage_chunk<MODE>(S, sorted, pair_val, s0 + base, cnt, std2, max_splats);
+            stage_chunk<MODE>(S, sorted, pairs, s0 + base, cnt, std2, max_splats);
             __syncthreads();
             if (__any_sync(0xFFFFFFFFu, !found)) {
                 const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
@@ -403,7 +408,7 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
             for (uint32_t base = kmin / kRasterThreads * kRasterThreads; base < n; base += kRasterThreads) {
                 const uint32_t cnt = min(kRasterThreads, n - base);
                 __syncthreads();
-                stage_chunk<MODE>(S, sorted, pair_val, s0 + base, cnt, std2, max_splats);
+                stage_chunk<MODE>(S, sorted, pairs, s0 + base, cnt, std2, max_splats);
                 __syncthreads();
                 if (__any_sync(0xFFFFFFFFu, active)) {
                     const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
@@ -447,10 +452,10 @@ static void launch_raster_mode(const RasterLayout &L, uint8_t *target, uint32_t 
     const RasterTuning t = raster_tuning();
     if (exact)
         raster_kernel<MODE, true><<<L.ntiles, kRasterThreads, 0, st>>>(
-            L.sorted, L.pair_val, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
+            L.sorted, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
     else
         raster_kernel<MODE, false><<<L.ntiles, kRasterThreads, 0, st>>>(
-            L.sorted, L.pair_val, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
+            L.sorted, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
 }
 
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
@@ -462,6 +467,10 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     if (L.ntiles == 0) return cudaSuccess;
     ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1);
     count_launches(1);
+    cudaError_t e = sort_pairs_begin(L.sort_scratch, st);
+    if (e != cudaSuccess) return e;
+    Ctrl *sort_ctrl = sort_pairs_ctrl(L.sort_scratch);
+    const uint32_t key_passes = (L.key_bits + 7u) / 8u;
     uint32_t rank_offset = 0;
     prof_mark(kProfBin, true, st);
     for (uint32_t s = 0; s < nseg; ++s) {
@@ -470,18 +479,20 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
             count_launches(1);
         }
         const uint32_t blocks = (segs[s].max_count + kBinThreads - 1) / kBinThreads;
-        if (blocks > 0) count_launches(1);
-        if (blocks > 0)
+        if (blocks > 0) {
             bin_kernel<<<blocks, kBinThreads, 0, st>>>(segs[s].splats, segs[s].sorted_index, segs[s].count,
-                                                       segs[s].max_count, rank_offset, L.sorted, L.pair_key,
-                                                       L.pair_val, max_pairs, L.tiles_x, L.tiles_y, L.ctrl, L.flags);
+                                                       segs[s].max_count, rank_offset, L.sorted, L.pairs, max_pairs,
+                                                       L.tiles_x, L.tiles_y, L.ctrl, L.flags, sort_ctrl, key_passes);
+            count_launches(1);
+        }
         rank_offset += segs[s].max_count;
     }
     prof_mark(kProfBin, false, st);
-    cudaError_t e = launch_sort(L.pair_key, L.pair_val, max_pairs, &L.ctrl->count, L.key_bits, L.sort_scratch, st,
-                                kProfTileSort);
+    prof_mark(kProfTileSort, true, st);
+    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_scratch, st);
+    prof_mark(kProfTileSort, false, st);
     if (e != cudaSuccess) return e;
-    merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, reinterpret_cast<const Ctrl *>(L.sort_scratch));
+    merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, sort_ctrl);
     count_launches(1);
     e = cudaMemsetAsync(L.ranges, 0, (size_t)L.ntiles * sizeof(uint2), st);
     if (e != cudaSuccess) return e;
@@ -489,7 +500,7 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     if (rblocks > 152 * 8) rblocks = 152 * 8;
     if (rblocks == 0) rblocks = 1;
     prof_mark(kProfRanges, true, st);
-    tile_ranges_kernel<<<rblocks, 256, 0, st>>>(L.pair_key, L.ctrl, L.ranges, L.ntiles);
+    tile_ranges_kernel<<<rblocks, 256, 0, st>>>(L.pairs, L.ctrl, L.ranges, L.ntiles);
     prof_mark(kProfRanges, false, st);
     count_launches(1);
     const float std2 = u.std_dev * u.std_dev;

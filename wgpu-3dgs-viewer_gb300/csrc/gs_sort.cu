@@ -102,12 +102,52 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, u
     return before + x - v;
 }
 
-__global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(
-    const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint32_t *__restrict__ kout,
-    uint32_t *__restrict__ vout, const uint32_t *count, uint32_t max_count, uint32_t pass, Ctrl *ctrl,
-    uint64_t *flags) {
-    __shared__ uint32_t s_keys[kTileKeys];
-    __shared__ uint32_t s_vals[kTileKeys];
+// Look-back of one digit counter (flags[j * 256], j < tile) that polls up to four
+// predecessors per round trip.  The flag word carries everything the reader uses, so relaxed
+// loads suffice.  Returns the exclusive prefix; on timeout sets the status bit.
+__device__ __forceinline__ uint32_t look_back_digit(const uint64_t *flags, uint32_t tile, uint32_t epoch,
+                                                    uint32_t *status) {
+    uint32_t prefix = 0;
+    int64_t j = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+        uint64_t w[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) w[q] = (j - q >= 0) ? ld_relaxed(flags + (uint64_t)(j - q) * 256u) : 0ull;
+        bool stalled = false, done = false;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            if (stalled || done || j < 0) continue;
+            const uint32_t st = (uint32_t)(w[q] >> 32) & 3u;
+            if ((uint32_t)(w[q] >> 34) != epoch || st == 0u) {
+                stalled = true;
+                continue;
+            }
+            prefix += (uint32_t)w[q];
+            if (st == kFlagPrefix) done = true;
+            else --j;
+        }
+        if (done) break;
+        if (stalled) {
+            if (++spins > kSpinLimit) {
+                atomicOr(status, kStatusTimeout);
+                break;
+            }
+            if (spins > 64) __nanosleep(32);
+        }
+    }
+    return prefix;
+}
+
+// One LSD pass over the digit at `shift`.  Input and output are either split (keys[],
+// values[]) or packed (uint2 {key, value}); packed ping-pong buffers keep each digit's run of
+// 8-byte pairs contiguous in the scatter.
+template <bool IN_PACKED, bool OUT_PACKED>
+__global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
+    const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
+    uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
+    uint32_t max_count, uint32_t pass, Ctrl *ctrl, uint64_t *flags) {
+    __shared__ uint2 s_kv[kTileKeys];
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_start[256];
     __shared__ uint32_t s_gbase[256];
@@ -128,13 +168,19 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(
     const uint32_t shift = 8u * pass;
     const uint32_t base = tile * kTileKeys + warp * (32u * kSortRows);
 
-    uint32_t k[kSortRows], v[kSortRows], r[kSortRows];
+    uint32_t k[kSortRows], r[kSortRows];
+    uint32_t v[IN_PACKED ? kSortRows : 1];
 #pragma unroll
     for (uint32_t i = 0; i < kSortRows; ++i) {
         const uint32_t pos = base + i * 32u + lane;
         const bool ok = pos < n;
-        k[i] = ok ? kin[pos] : 0xFFFFFFFFu;
-        v[i] = ok ? vin[pos] : 0u;
+        if constexpr (IN_PACKED) {
+            const uint2 kv = ok ? pin[pos] : make_uint2(0xFFFFFFFFu, 0u);
+            k[i] = kv.x;
+            v[i] = kv.y;
+        } else {
+            k[i] = ok ? kin[pos] : 0xFFFFFFFFu;
+        }
     }
     // Warp-local stable ranking: lanes that share a digit form a peer mask from 8 ballots.
     const uint32_t lt = lanemask_lt();
@@ -170,87 +216,119 @@ __global__ void __launch_bounds__(kSortThreads) sort_pass_kernel(
     const uint32_t invalid = (tile == ntiles - 1) ? ntiles * kTileKeys - n : 0u;
     const uint32_t pub = (d == 255u) ? total - invalid : total;
     uint64_t *f = flags + (size_t)tile * 256u + d;
-    if (tile == 0)
-        st_release(f, pack_flag(epoch, kFlagPrefix, pub));
-    else
-        st_release(f, pack_flag(epoch, kFlagAggregate, pub));
+    st_relaxed(f, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
 
     uint32_t blk_total, hist_total;
     const uint32_t start = block_scan_excl(total, s_tmp, &blk_total);
     const uint32_t goff = block_scan_excl(ctrl->hist[pass][d], s_tmp, &hist_total);
     uint32_t prefix = 0;
     if (tile > 0) {
-        prefix = look_back(flags + d, 256u, tile, epoch, &ctrl->status);
-        st_release(f, pack_flag(epoch, kFlagPrefix, prefix + pub));
+        prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status);
+        st_relaxed(f, pack_flag(epoch, kFlagPrefix, prefix + pub));
     }
     s_start[d] = start;
     s_gbase[d] = goff + prefix;
     __syncthreads();
 
+    if constexpr (IN_PACKED) {
 #pragma unroll
-    for (uint32_t i = 0; i < kSortRows; ++i) {
-        const uint32_t dd = (k[i] >> shift) & 255u;
-        const uint32_t p = s_start[dd] + s_whist[warp][dd] + r[i];
-        s_keys[p] = k[i];
-        s_vals[p] = v[i];
+        for (uint32_t i = 0; i < kSortRows; ++i) {
+            const uint32_t dd = (k[i] >> shift) & 255u;
+            s_kv[s_start[dd] + s_whist[warp][dd] + r[i]] = make_uint2(k[i], v[i]);
+        }
+    } else {
+        // Values are read only now, after ranking, which keeps them out of registers above.
+#pragma unroll
+        for (uint32_t i = 0; i < kSortRows; ++i) {
+            const uint32_t pos = base + i * 32u + lane;
+            const uint32_t vv = pos < n ? vin[pos] : 0u;
+            const uint32_t dd = (k[i] >> shift) & 255u;
+            s_kv[s_start[dd] + s_whist[warp][dd] + r[i]] = make_uint2(k[i], vv);
+        }
     }
     __syncthreads();
     const uint32_t valid = min(kTileKeys, n - tile * kTileKeys);
     for (uint32_t j = tid; j < valid; j += kSortThreads) {
-        const uint32_t key = s_keys[j];
-        const uint32_t dd = (key >> shift) & 255u;
+        const uint2 kv = s_kv[j];
+        const uint32_t dd = (kv.x >> shift) & 255u;
         const uint32_t o = s_gbase[dd] + (j - s_start[dd]);
         if (o < n) {  // always true unless a look-back timed out (status already set)
-            kout[o] = key;
-            vout[o] = s_vals[j];
+            if constexpr (OUT_PACKED) {
+                pout[o] = kv;
+            } else {
+                kout[o] = kv.x;
+                vout[o] = kv.y;
+            }
         }
     }
 }
 
-__global__ void copy_pairs_kernel(const uint32_t *ks, const uint32_t *vs, uint32_t *kd, uint32_t *vd,
-                                  const uint32_t *count, uint32_t max_count) {
+__global__ void unpack_pairs_kernel(const uint2 *src, uint32_t *kd, uint32_t *vd, const uint32_t *count,
+                                    uint32_t max_count) {
     const uint32_t n = load_count(count, max_count);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        kd[i] = ks[i];
-        vd[i] = vs[i];
+        const uint2 kv = src[i];
+        kd[i] = kv.x;
+        vd[i] = kv.y;
     }
+}
+
+__global__ void copy_packed_kernel(const uint2 *src, uint2 *dst, const uint32_t *count, uint32_t max_count) {
+    const uint32_t n = load_count(count, max_count);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = src[i];
 }
 
 static inline uint32_t sort_passes(uint32_t key_bits) { return (key_bits + 7u) / 8u; }
 
 struct SortLayout {
     Ctrl *ctrl;
-    uint32_t *kalt, *valt;
+    uint2 *alt_a, *alt_b;
     uint64_t *flags;
     uint32_t ntiles;
 };
 
-static SortLayout sort_layout(void *scratch, uint32_t max_count) {
+// Scratch: control block | packed buffer A | packed buffer B (split sorts of 3+ passes only) |
+// look-back flags [passes][tiles][256].
+static size_t sort_tiles(uint32_t max_count) {
+    size_t t = (max_count + kTileKeys - 1) / kTileKeys;
+    return t ? t : 1;
+}
+
+static SortLayout sort_layout(void *scratch, uint32_t max_count, uint32_t npasses) {
     SortLayout L;
     uint8_t *p = reinterpret_cast<uint8_t *>(scratch);
-    L.ntiles = (max_count + kTileKeys - 1) / kTileKeys;
-    if (L.ntiles == 0) L.ntiles = 1;
+    L.ntiles = (uint32_t)sort_tiles(max_count);
     L.ctrl = reinterpret_cast<Ctrl *>(p);
     p += align_up(sizeof(Ctrl), 256);
-    L.kalt = reinterpret_cast<uint32_t *>(p);
-    p += align_up((size_t)max_count * 4, 256);
-    L.valt = reinterpret_cast<uint32_t *>(p);
-    p += align_up((size_t)max_count * 4, 256);
+    L.alt_a = reinterpret_cast<uint2 *>(p);
+    p += align_up((size_t)max_count * 8, 256);
+    L.alt_b = reinterpret_cast<uint2 *>(p);
+    if (npasses >= 3) p += align_up((size_t)max_count * 8, 256);
     L.flags = reinterpret_cast<uint64_t *>(p);
     return L;
 }
 
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits) {
-    size_t ntiles = (max_count + kTileKeys - 1) / kTileKeys;
-    if (ntiles == 0) ntiles = 1;
-    return align_up(sizeof(Ctrl), 256) + 2 * align_up((size_t)max_count * 4, 256) +
-           (size_t)sort_passes(key_bits) * ntiles * 256 * sizeof(uint64_t);
+    const uint32_t np = sort_passes(key_bits);
+    return align_up(sizeof(Ctrl), 256) + (np >= 3 ? 2 : 1) * align_up((size_t)max_count * 8, 256) +
+           (size_t)np * sort_tiles(max_count) * 256 * sizeof(uint64_t);
+}
+
+size_t sort_pairs_scratch_bytes(uint32_t max_count, uint32_t key_bits) {
+    return align_up(sizeof(Ctrl), 256) + align_up((size_t)max_count * 8, 256) +
+           (size_t)sort_passes(key_bits) * sort_tiles(max_count) * 256 * sizeof(uint64_t);
+}
+
+static uint32_t grid_for(uint32_t max_count) {
+    uint32_t blocks = (max_count + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    return blocks ? blocks : 1;
 }
 
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage) {
-    const SortLayout L = sort_layout(scratch, max_count);
     const uint32_t npasses = sort_passes(key_bits);
+    const SortLayout L = sort_layout(scratch, max_count, npasses);
     ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1);
     count_launches(1);
     if (max_count == 0) return cudaGetLastError();
@@ -258,25 +336,60 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     uint32_t hist_blocks = (max_count + 256 * 16 - 1) / (256 * 16);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
     sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, npasses, L.ctrl);
-    uint32_t *ka = keys, *va = vals, *kb = L.kalt, *vb = L.valt;
-    for (uint32_t p = 0; p < npasses; ++p) {
-        sort_pass_kernel<<<L.ntiles, kSortThreads, 0, st>>>(ka, va, kb, vb, count, max_count, p, L.ctrl,
-                                                           L.flags + (size_t)p * L.ntiles * 256);
-        uint32_t *t = ka;
-        ka = kb;
-        kb = t;
-        t = va;
-        va = vb;
-        vb = t;
+    count_launches(1);
+    const size_t fstride = (size_t)L.ntiles * 256;
+    if (npasses == 1) {
+        sort_pass_kernel<false, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, L.alt_a,
+                                                                        count, max_count, 0, L.ctrl, L.flags);
+        unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
+        count_launches(2);
+    } else {
+        uint2 *src = L.alt_a, *dst = L.alt_b;
+        sort_pass_kernel<false, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, src,
+                                                                        count, max_count, 0, L.ctrl, L.flags);
+        for (uint32_t p = 1; p + 1 < npasses; ++p) {
+            sort_pass_kernel<true, true><<<L.ntiles, kSortThreads, 0, st>>>(
+                nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, L.ctrl, L.flags + p * fstride);
+            uint2 *t = src;
+            src = dst;
+            dst = t;
+        }
+        sort_pass_kernel<true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, keys, vals, nullptr, count,
+                                                                        max_count, npasses - 1, L.ctrl,
+                                                                        L.flags + (npasses - 1) * fstride);
+        count_launches(npasses);
     }
+    prof_mark(prof_stage, false, st);
+    return cudaGetLastError();
+}
+
+Ctrl *sort_pairs_ctrl(void *scratch) { return reinterpret_cast<Ctrl *>(scratch); }
+
+cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st) {
+    ctrl_init_kernel<<<1, 256, 0, st>>>(reinterpret_cast<Ctrl *>(scratch), 1);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits,
+                              void *scratch, cudaStream_t st) {
+    const uint32_t npasses = sort_passes(key_bits);
+    if (max_count == 0) return cudaSuccess;
+    SortLayout L = sort_layout(scratch, max_count, 1);
+    const size_t fstride = (size_t)L.ntiles * 256;
+    uint2 *src = data, *dst = L.alt_a;
+    for (uint32_t p = 0; p < npasses; ++p) {
+        sort_pass_kernel<true, true><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
+                                                                       count, max_count, p, L.ctrl, L.flags + p * fstride);
+        uint2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    count_launches(npasses);
     if (npasses & 1u) {
-        uint32_t blocks = (max_count + 255) / 256;
-        if (blocks > 152 * 8) blocks = 152 * 8;
-        copy_pairs_kernel<<<blocks, 256, 0, st>>>(ka, va, keys, vals, count, max_count);
+        copy_packed_kernel<<<grid_for(max_count), 256, 0, st>>>(src, data, count, max_count);
         count_launches(1);
     }
-    count_launches(1 + npasses);
-    prof_mark(prof_stage, false, st);
     return cudaGetLastError();
 }
 
