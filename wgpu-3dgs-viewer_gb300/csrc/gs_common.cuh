@@ -26,7 +26,8 @@ struct Ctrl {
     uint32_t count;       // preprocess: V; raster: tile pairs kept
     uint32_t total;       // raster: tile pairs wanted (saturating)
     uint32_t pair_base;   // raster: running pair offset across segments
-    uint32_t pad[3];
+    uint32_t seg_total;   // raster: pairs of the segment being binned
+    uint32_t pad[2];
     uint32_t hist[4][256];  // sort: global digit histograms
 };
 static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl must keep 16-byte alignment of what follows");

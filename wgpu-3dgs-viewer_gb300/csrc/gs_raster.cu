@@ -26,18 +26,27 @@ constexpr uint32_t kRasterThreads = 256;
 
 struct RasterLayout {
     Ctrl *ctrl;
-    gs_splat *sorted;    // draw-ordered splats, capacity max_splats
-    uint64_t *flags;     // bin look-back flags, ceil(max_splats / 256)
-    uint2 *pairs;        // (tile, draw rank), capacity max_pairs
+    gs_splat *sorted;    // draw-ordered splats (several models), capacity max_splats
+    uint4 *info;         // per draw rank: tile rectangle, kept-tile mask, pair value
+    uint32_t *offsets;   // per draw rank: tile count, then its exclusive scan
+    uint64_t *flags;     // scan look-back flags
+    uint2 *pairs;        // (tile, value), capacity max_pairs
     uint2 *ranges;       // per tile [start, end)
     void *sort_scratch;
     uint32_t tiles_x, tiles_y, ntiles, key_bits;
 };
 
+constexpr uint32_t kScanItems = 16;
+constexpr uint32_t kScanTile = 256 * kScanItems;
+
 static uint32_t bits_for(uint32_t v) {
     uint32_t b = 1;
     while (b < 32 && (v >> b) != 0) ++b;
     return b;
+}
+
+static size_t scan_flag_bytes(uint32_t max_splats) {
+    return align_up(((size_t)max_splats + kScanTile - 1) / kScanTile * 8 + 8, 256);
 }
 
 static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w, uint32_t h,
@@ -52,8 +61,12 @@ static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w
     p += align_up(sizeof(Ctrl), 256);
     L.sorted = reinterpret_cast<gs_splat *>(p);
     p += align_up((size_t)max_splats * sizeof(gs_splat), 256);
+    L.info = reinterpret_cast<uint4 *>(p);
+    p += align_up((size_t)max_splats * 16, 256);
+    L.offsets = reinterpret_cast<uint32_t *>(p);
+    p += align_up((size_t)max_splats * 4 + 16, 256);
     L.flags = reinterpret_cast<uint64_t *>(p);
-    p += align_up(((size_t)max_splats + kBinThreads - 1) / kBinThreads * 8 + 8, 256);
+    p += scan_flag_bytes(max_splats);
     L.pairs = reinterpret_cast<uint2 *>(p);
     p += align_up((size_t)max_pairs * 8, 256);
     L.ranges = reinterpret_cast<uint2 *>(p);
@@ -66,9 +79,9 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_
     const uint32_t tiles = ((w + GS_TILE - 1) / GS_TILE) * ((h + GS_TILE - 1) / GS_TILE);
     const uint32_t key_bits = bits_for(tiles > 0 ? tiles - 1 : 0);
     return align_up(sizeof(Ctrl), 256) + align_up((size_t)max_splats * sizeof(gs_splat), 256) +
-           align_up(((size_t)max_splats + kBinThreads - 1) / kBinThreads * 8 + 8, 256) +
-           align_up((size_t)max_pairs * 8, 256) + align_up((size_t)tiles * sizeof(uint2), 256) +
-           sort_pairs_scratch_bytes(max_pairs, key_bits);
+           align_up((size_t)max_splats * 16, 256) + align_up((size_t)max_splats * 4 + 16, 256) +
+           scan_flag_bytes(max_splats) + align_up((size_t)max_pairs * 8, 256) +
+           align_up((size_t)tiles * sizeof(uint2), 256) + sort_pairs_scratch_bytes(max_pairs, key_bits);
 }
 
 const Ctrl *raster_ctrl(const void *scratch) { return reinterpret_cast<const Ctrl *>(scratch); }
@@ -107,93 +120,212 @@ __device__ __forceinline__ bool tile_rect(const float4 a, uint32_t tiles_x, uint
     return true;
 }
 
-// K3: gather into draw order + count tiles + scan + emit (tile, rank) pairs.
-__global__ void __launch_bounds__(kBinThreads) bin_kernel(
+// Conservative test whether a splat's fragment ellipse {p : |Q·(p - c)|² <= r2} meets the 16x16
+// tiles of a rectangle.  A tile's box of pixel centres maps to a parallelogram in quad-offset
+// space with the same two edge vectors for every tile; the ellipse becomes the disc of radius
+// sqrt(r2) about the origin, which lies outside the parallelogram when c lies outside the box,
+// so the two meet iff an edge comes within the radius.  The limit carries a small margin, so
+// rounding can only keep a tile, never drop one.
+struct TileCull {
+    float cx, cy, q0, q1, q2, q3, e1x, e1y, e2x, e2y, i1, i2, lim;
+
+    __device__ __forceinline__ TileCull(const float4 a, const float4 q, float r2) {
+        cx = a.x;
+        cy = a.y;
+        q0 = q.x;
+        q1 = q.y;
+        q2 = q.z;
+        q3 = q.w;
+        const float side = (float)(GS_TILE - 1);
+        e1x = q.x * side;
+        e1y = q.z * side;
+        e2x = q.y * side;
+        e2y = q.w * side;
+        i1 = __frcp_rn(e1x * e1x + e1y * e1y);
+        i2 = __frcp_rn(e2x * e2x + e2y * e2y);
+        lim = r2 * 1.002f + 1e-4f;
+    }
+
+    __device__ __forceinline__ bool edge(float ux, float uy, float ex, float ey, float inv) const {
+        float t = -(ux * ex + uy * ey) * inv;
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+        const float px = ux + t * ex, py = uy + t * ey;
+        return px * px + py * py <= lim;
+    }
+
+    // Tile whose first pixel centre is (x0, y0).  Only box edges facing the centre can hold
+    // the point nearest to it, and a linear map keeps which side of an edge a point lies on.
+    __device__ __forceinline__ bool meets(float x0, float y0) const {
+        const float x1 = x0 + (float)(GS_TILE - 1), y1 = y0 + (float)(GS_TILE - 1);
+        const float dx = x0 - cx, dy = y0 - cy;
+        const float ux = q0 * dx + q1 * dy, uy = q2 * dx + q3 * dy;  // corner (x0, y0)
+        if (cx < x0 && edge(ux, uy, e2x, e2y, i2)) return true;                  // left edge
+        if (cx > x1 && edge(ux + e1x, uy + e1y, e2x, e2y, i2)) return true;      // right edge
+        if (cy < y0 && edge(ux, uy, e1x, e1y, i1)) return true;                  // top edge
+        if (cy > y1 && edge(ux + e2x, uy + e2y, e1x, e1y, i1)) return true;      // bottom edge
+        return cx >= x0 && cx <= x1 && cy >= y0 && cy <= y1;                     // centre inside
+    }
+};
+
+// K3a: per draw rank, the splat's tile rectangle, the corner tiles its footprint misses, and
+// its tile count.  Several models first copy their splats into draw order.
+__global__ void __launch_bounds__(kBinThreads) bin_count_kernel(
     const gs_splat *__restrict__ splats, const uint32_t *__restrict__ sorted_index, const uint32_t *count,
-    uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, uint2 *__restrict__ pairs,
-    uint32_t max_pairs, uint32_t tiles_x, uint32_t tiles_y, Ctrl *ctrl, uint64_t *flags, Ctrl *sort_ctrl,
-    uint32_t key_passes) {
-    __shared__ uint32_t s_incl[kBinThreads];
-    __shared__ uint32_t s_x0[kBinThreads], s_y0[kBinThreads], s_w[kBinThreads];
-    __shared__ uint32_t s_tmp[kBinThreads / 32];
-    __shared__ uint32_t s_tile, s_epoch, s_base, s_seg_base, s_seg_want;
-    __shared__ uint32_t s_hist[4][256];  // digit histograms of the emitted tile ids (tile sort)
+    uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, int direct, uint32_t tiles_x,
+    uint32_t tiles_y, uint32_t mode, float std2, uint4 *__restrict__ info, uint32_t *__restrict__ counts) {
+    const uint32_t n = count ? min(*count, max_count) : max_count;
+    const uint32_t k = blockIdx.x * kBinThreads + threadIdx.x;
+    if (k >= n) return;
+    // Indices come from the depth sort; the bound check only matters if that sort timed out.
+    const uint32_t gi = sorted_index[k];
+    uint32_t cnt = 0, x0 = 0, y0 = 0, w = 0, h = 0, mask = 0;
+    if (gi < max_count) {
+        const float4 *src = reinterpret_cast<const float4 *>(splats + gi);
+        const float4 a = __ldg(src);
+        const float4 q = __ldg(src + 1);
+        if (!direct) {
+            float4 *dst = reinterpret_cast<float4 *>(sorted_out + rank_offset + k);
+            dst[0] = a;
+            dst[1] = q;
+            dst[2] = __ldg(src + 2);
+        }
+        if (tile_rect(a, tiles_x, tiles_y, &x0, &y0, &w, &h)) {
+            cnt = w * h;
+            // The footprint is convex and its box meets every tile of the rectangle, so only the
+            // corner tiles of a rectangle (up to 16 tiles) can miss it; drop those that do.
+            if (mode != GS_DISPLAY_POINT && cnt > 1 && cnt <= 16) {
+                const float r2 = (mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(__ldg(&src[2].w), std2) : std2;
+                const TileCull cull(a, q, r2);
+                mask = cnt == 16 ? 0xFFFFu : (1u << cnt) - 1u;
+#pragma unroll
+                for (uint32_t c = 0; c < 4; ++c) {
+                    const uint32_t tx = (c & 1u) ? w - 1 : 0u, ty = (c & 2u) ? h - 1 : 0u;
+                    if (((c & 1u) && w == 1) || ((c & 2u) && h == 1)) continue;  // same tile again
+                    if (!cull.meets((float)((x0 + tx) * GS_TILE) + 0.5f, (float)((y0 + ty) * GS_TILE) + 0.5f))
+                        mask &= ~(1u << (ty * w + tx));
+                }
+                cnt = __popc(mask);
+            }
+        }
+    }
+    info[k] = make_uint4(x0 | (y0 << 16), w | (h << 16), mask, direct ? gi : rank_offset + k);
+    counts[k] = cnt;
+}
+
+// K3b: exclusive scan of the tile counts in place (decoupled look-back over 4096-count tiles);
+// the last tile records the segment's total.
+__global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ data, const uint32_t *count,
+                                                       uint32_t max_count, Ctrl *ctrl, uint64_t *flags) {
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_tile, s_epoch, s_prefix;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    for (uint32_t i = tid; i < 4 * 256; i += kBinThreads) (&s_hist[0][0])[i] = 0u;
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
-        s_seg_base = *(volatile uint32_t *)&ctrl->pair_base;
-        s_seg_want = *(volatile uint32_t *)&ctrl->total;
-        s_tile = atomicAdd(&ctrl->ticket[0], 1u);
+        s_tile = atomicAdd(&ctrl->ticket[1], 1u);
     }
     __syncthreads();
     const uint32_t n = count ? min(*count, max_count) : max_count;
-    const uint32_t ntiles = (n + kBinThreads - 1) / kBinThreads;
+    const uint32_t ntiles = (n + kScanTile - 1) / kScanTile;
     const uint32_t tile = s_tile, epoch = s_epoch;
     if (tile >= ntiles) return;
-    const uint32_t k = tile * kBinThreads + tid;
-    uint32_t cnt = 0, x0 = 0, y0 = 0, w = 0, h = 0;
-    // Indices come from the depth sort; the bound check only matters if that sort timed out.
-    const uint32_t gi = k < n ? sorted_index[k] : 0xFFFFFFFFu;
-    if (gi < max_count) {
-        const float4 *src = reinterpret_cast<const float4 *>(splats + gi);
-        const float4 a = __ldg(src), b = __ldg(src + 1), c = __ldg(src + 2);
-        float4 *dst = reinterpret_cast<float4 *>(sorted_out + rank_offset + k);
-        dst[0] = a;
-        dst[1] = b;
-        dst[2] = c;
-        if (tile_rect(a, tiles_x, tiles_y, &x0, &y0, &w, &h)) cnt = w * h;
+    const uint32_t base = tile * kScanTile + tid * kScanItems;
+    uint32_t v[kScanItems];
+    if (base + kScanItems <= n) {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; i += 4) {
+            const uint4 x = *reinterpret_cast<const uint4 *>(data + base + i);
+            v[i] = x.x;
+            v[i + 1] = x.y;
+            v[i + 2] = x.z;
+            v[i + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) v[i] = base + i < n ? data[base + i] : 0u;
     }
-    // Block inclusive scan of the tile counts.
-    uint32_t x = cnt;
+    uint32_t sum = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kScanItems; ++i) sum += v[i];
+    uint32_t x = sum;
 #pragma unroll
     for (uint32_t o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
         if (lane >= o) x += y;
     }
-    if (lane == 31) s_tmp[warp] = x;
+    if (lane == 31) s_warp[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        uint32_t run = 0, mine = 0;
-        for (uint32_t i = 0; i < kBinThreads / 32; ++i) {
-            const uint32_t c = s_tmp[i];
-            if (lane == i) mine = run;
-            run += c;
+        uint32_t wv = lane < 8 ? s_warp[lane] : 0u;
+        uint32_t wi = wv;
+#pragma unroll
+        for (uint32_t o = 1; o < 8; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, wi, o);
+            if (lane >= o) wi += y;
         }
-        const uint32_t total = run;
-        if (lane == 0)
-            st_release(flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, total));
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, wi, 7);
+        if (lane == 0) st_relaxed(flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, total));
         const uint32_t prefix = tile == 0 ? 0u : look_back_warp(flags, tile, epoch, &ctrl->status);
-        __syncwarp();
-        if (lane < kBinThreads / 32) s_tmp[lane] = mine;
+        if (lane < 8) s_warp[lane] = wi - wv;  // exclusive per-warp offsets
         if (lane == 0) {
-            if (tile > 0) {
-                const uint64_t incl = (uint64_t)prefix + total;
-                st_release(flags + tile,
-                           pack_flag(epoch, kFlagPrefix, incl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)incl));
-            }
-            s_base = prefix;
-            if (tile == ntiles - 1) {
-                const uint64_t want = (uint64_t)s_seg_want + prefix + total;
-                const uint32_t kept = want > max_pairs ? max_pairs : (uint32_t)want;
-                if (want > max_pairs) atomicOr(&ctrl->status, kStatusCapacity);
-                ctrl->total = want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want;
-                ctrl->count = kept;
-                ctrl->pair_base = kept;
-            }
+            const uint64_t incl = (uint64_t)prefix + total;
+            const uint32_t sat = incl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)incl;
+            if (tile > 0) st_relaxed(flags + tile, pack_flag(epoch, kFlagPrefix, sat));
+            s_prefix = prefix;
+            if (tile == ntiles - 1) ctrl->seg_total = sat;
         }
     }
     __syncthreads();
-    const uint32_t incl = s_tmp[warp] + x;
-    s_incl[tid] = incl;
-    s_x0[tid] = x0;
-    s_y0[tid] = y0;
-    s_w[tid] = w;
+    uint32_t run = s_prefix + s_warp[warp] + x - sum;
+    if (base + kScanItems <= n) {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; i += 4) {
+            uint4 o;
+            o.x = run;
+            run += v[i];
+            o.y = run;
+            run += v[i + 1];
+            o.z = run;
+            run += v[i + 2];
+            o.w = run;
+            run += v[i + 3];
+            *reinterpret_cast<uint4 *>(data + base + i) = o;
+        }
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < kScanItems; ++i) {
+            if (base + i < n) data[base + i] = run;
+            run += v[i];
+        }
+    }
+}
+
+// K3c: emission of the (tile, value) pairs of 256 draw ranks, load-balanced over the CTA, plus
+// the digit histograms of the tile ids for the tile sort.
+__global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
+    const uint4 *__restrict__ info, const uint32_t *__restrict__ offsets, const uint32_t *count, uint32_t max_count,
+    uint2 *__restrict__ pairs, uint32_t max_pairs, uint32_t tiles_x, const Ctrl *ctrl, Ctrl *sort_ctrl,
+    uint32_t key_passes) {
+    __shared__ uint32_t s_incl[kBinThreads];
+    __shared__ uint4 s_info[kBinThreads];
+    __shared__ uint32_t s_hist[4][256];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t n = count ? min(*count, max_count) : max_count;
+    const uint32_t k0 = blockIdx.x * kBinThreads;
+    if (k0 >= n) return;
+    for (uint32_t i = tid; i < 4 * 256; i += kBinThreads) (&s_hist[0][0])[i] = 0u;
+    const uint32_t seg_total = ctrl->seg_total;
+    const uint32_t first = offsets[k0];
+    const uint32_t k = k0 + tid;
+    // inclusive count of this rank, relative to the CTA's first pair
+    const uint32_t next = (k + 1 < n) ? offsets[k + 1] : seg_total;
+    s_incl[tid] = (k < n) ? next - first : 0u;
+    if (k < n) s_info[tid] = info[k];
     __syncthreads();
-    const uint32_t block_pairs = s_incl[kBinThreads - 1];
-    const uint64_t out0 = (uint64_t)s_seg_base + s_base;
-    // Load-balanced emission: pair j of the block belongs to the first thread whose
-    // inclusive count exceeds j.
+    const uint32_t last = min(kBinThreads, n - k0) - 1;
+    const uint32_t block_pairs = s_incl[last];
+    for (uint32_t t = last + 1 + tid; t < kBinThreads; t += kBinThreads) s_incl[t] = block_pairs;
+    __syncthreads();
+    const uint64_t out0 = (uint64_t)ctrl->pair_base + first;
     for (uint32_t j = tid; j < block_pairs; j += kBinThreads) {
         uint32_t lo = 0, hi = kBinThreads - 1;
         while (lo < hi) {
@@ -201,14 +333,18 @@ __global__ void __launch_bounds__(kBinThreads) bin_kernel(
             if (s_incl[mid] > j) hi = mid; else lo = mid + 1;
         }
         const uint32_t owner = lo;
-        const uint32_t excl = owner ? s_incl[owner - 1] : 0u;
-        const uint32_t r = j - excl;
-        const uint32_t ww = s_w[owner];
-        const uint32_t tyy = s_y0[owner] + r / ww, txx = s_x0[owner] + r % ww;
+        uint32_t r = j - (owner ? s_incl[owner - 1] : 0u);
+        const uint4 in = s_info[owner];
+        if (in.z) {  // position of the r-th kept tile in the rectangle
+            uint32_t m = in.z;
+            for (uint32_t i = 0; i < r; ++i) m &= m - 1u;
+            r = (uint32_t)(__ffs(m) - 1);
+        }
+        const uint32_t ww = in.y & 0xFFFFu;
+        const uint32_t t = ((in.x >> 16) + r / ww) * tiles_x + (in.x & 0xFFFFu) + r % ww;
         const uint64_t o = out0 + j;
         if (o < max_pairs) {
-            const uint32_t t = tyy * tiles_x + txx;
-            pairs[o] = make_uint2(t, rank_offset + tile * kBinThreads + owner);
+            pairs[o] = make_uint2(t, in.w);
             for (uint32_t p = 0; p < key_passes; ++p) atomicAdd(&s_hist[p][(t >> (8u * p)) & 255u], 1u);
         }
     }
@@ -219,14 +355,47 @@ __global__ void __launch_bounds__(kBinThreads) bin_kernel(
     }
 }
 
+// K3d: advance the running pair base past a segment; flags a tile-pair list overflow.
+__global__ void bin_advance_kernel(Ctrl *ctrl, const uint32_t *count, uint32_t max_count, uint32_t max_pairs) {
+    const uint32_t n = count ? min(*count, max_count) : max_count;
+    const uint64_t seg = n ? ctrl->seg_total : 0u;
+    const uint64_t want = (uint64_t)ctrl->total + seg;
+    const uint32_t sat = want > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)want;
+    const uint32_t kept = sat > max_pairs ? max_pairs : sat;
+    if (sat > max_pairs) ctrl->status |= kStatusCapacity;
+    ctrl->total = sat;
+    ctrl->count = kept;
+    ctrl->pair_base = kept;
+}
+
+// [start, end) of every tile's run in the tile-sorted pairs; each thread checks four
+// consecutive pairs with two 16-byte loads.
 __global__ void tile_ranges_kernel(const uint2 *__restrict__ pairs, const Ctrl *ctrl, uint2 *ranges,
                                    uint32_t ntiles) {
     const uint32_t n = ctrl->count;
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const uint32_t t = pairs[p].x;
-        if (t >= ntiles) continue;
-        if (p == 0 || pairs[p - 1].x != t) ranges[t].x = p;
-        if (p == n - 1 || pairs[p + 1].x != t) ranges[t].y = p + 1;
+    const uint32_t stride = gridDim.x * blockDim.x * 4u;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) * 4u; base < n; base += stride) {
+        uint32_t t[6];  // t[0] = previous pair, t[1..4] = this thread's pairs, t[5] = next pair
+        if (base + 4u <= n) {
+            const uint4 a = *reinterpret_cast<const uint4 *>(pairs + base);
+            const uint4 b = *reinterpret_cast<const uint4 *>(pairs + base + 2);
+            t[1] = a.x;
+            t[2] = a.z;
+            t[3] = b.x;
+            t[4] = b.z;
+        } else {
+            for (uint32_t i = 0; i < 4; ++i) t[1 + i] = base + i < n ? pairs[base + i].x : 0xFFFFFFFFu;
+        }
+        t[0] = base > 0 ? pairs[base - 1].x : 0xFFFFFFFFu;
+        t[5] = base + 4u < n ? pairs[base + 4].x : 0xFFFFFFFFu;
+#pragma unroll
+        for (uint32_t i = 1; i <= 4; ++i) {
+            const uint32_t p = base + i - 1;
+            const uint32_t k = t[i];
+            if (p >= n || k >= ntiles) continue;
+            if (t[i - 1] != k) ranges[k].x = p;
+            if (t[i + 1] != k) ranges[k].y = p + 1;
+        }
     }
 }
 
@@ -447,15 +616,16 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
 }
 
 template <uint32_t MODE>
-static void launch_raster_mode(const RasterLayout &L, uint8_t *target, uint32_t W, uint32_t H, uint32_t pitch,
-                               float std2, float outline2, int exact, uint32_t max_splats, cudaStream_t st) {
+static void launch_raster_mode(const RasterLayout &L, const gs_splat *splats, uint8_t *target, uint32_t W, uint32_t H,
+                               uint32_t pitch, float std2, float outline2, int exact, uint32_t max_splats,
+                               cudaStream_t st) {
     const RasterTuning t = raster_tuning();
     if (exact)
         raster_kernel<MODE, true><<<L.ntiles, kRasterThreads, 0, st>>>(
-            L.sorted, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
+            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
     else
         raster_kernel<MODE, false><<<L.ntiles, kRasterThreads, 0, st>>>(
-            L.sorted, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
+            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
 }
 
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
@@ -473,19 +643,25 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     const uint32_t key_passes = (L.key_bits + 7u) / 8u;
     uint32_t rank_offset = 0;
     prof_mark(kProfBin, true, st);
+    const int direct = nseg == 1 ? 1 : 0;
     for (uint32_t s = 0; s < nseg; ++s) {
+        const RasterSegment &g = segs[s];
+        const uint32_t blocks = (g.max_count + kBinThreads - 1) / kBinThreads;
+        if (blocks == 0) continue;
         if (s > 0) {
             ctrl_init_kernel<<<1, 32, 0, st>>>(L.ctrl, 0);
             count_launches(1);
         }
-        const uint32_t blocks = (segs[s].max_count + kBinThreads - 1) / kBinThreads;
-        if (blocks > 0) {
-            bin_kernel<<<blocks, kBinThreads, 0, st>>>(segs[s].splats, segs[s].sorted_index, segs[s].count,
-                                                       segs[s].max_count, rank_offset, L.sorted, L.pairs, max_pairs,
-                                                       L.tiles_x, L.tiles_y, L.ctrl, L.flags, sort_ctrl, key_passes);
-            count_launches(1);
-        }
-        rank_offset += segs[s].max_count;
+        bin_count_kernel<<<blocks, kBinThreads, 0, st>>>(g.splats, g.sorted_index, g.count, g.max_count, rank_offset,
+                                                         L.sorted, direct, L.tiles_x, L.tiles_y, u.display_mode,
+                                                         u.std_dev * u.std_dev, L.info, L.offsets);
+        const uint32_t scan_blocks = (g.max_count + kScanTile - 1) / kScanTile;
+        bin_scan_kernel<<<scan_blocks, 256, 0, st>>>(L.offsets, g.count, g.max_count, L.ctrl, L.flags);
+        bin_emit_kernel<<<blocks, kBinThreads, 0, st>>>(L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs,
+                                                        L.tiles_x, L.ctrl, sort_ctrl, key_passes);
+        bin_advance_kernel<<<1, 1, 0, st>>>(L.ctrl, g.count, g.max_count, max_pairs);
+        count_launches(4);
+        rank_offset += g.max_count;
     }
     prof_mark(kProfBin, false, st);
     prof_mark(kProfTileSort, true, st);
@@ -506,17 +682,20 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     const float std2 = u.std_dev * u.std_dev;
     const float o = u.std_dev - 0.1f;
     const float outline2 = o * o;
+    // Pair values index the model's own splat array (one segment) or the draw-ordered copy.
+    const gs_splat *rsplats = nseg == 1 ? segs[0].splats : L.sorted;
+    const uint32_t rmax = nseg == 1 ? segs[0].max_count : max_splats;
     prof_mark(kProfRaster, true, st);
     count_launches(1);
     switch (u.display_mode) {
         case GS_DISPLAY_SPLAT:
-            launch_raster_mode<GS_DISPLAY_SPLAT>(L, target, W, H, pitch, std2, outline2, exact_exp, max_splats, st);
+            launch_raster_mode<GS_DISPLAY_SPLAT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st);
             break;
         case GS_DISPLAY_ELLIPSE:
-            launch_raster_mode<GS_DISPLAY_ELLIPSE>(L, target, W, H, pitch, std2, outline2, exact_exp, max_splats, st);
+            launch_raster_mode<GS_DISPLAY_ELLIPSE>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st);
             break;
         default:
-            launch_raster_mode<GS_DISPLAY_POINT>(L, target, W, H, pitch, std2, outline2, exact_exp, max_splats, st);
+            launch_raster_mode<GS_DISPLAY_POINT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st);
             break;
     }
     prof_mark(kProfRaster, false, st);

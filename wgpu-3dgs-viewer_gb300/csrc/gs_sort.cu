@@ -26,12 +26,14 @@ __global__ void ctrl_init_kernel(Ctrl *ctrl, int mode) {
         if (e >= (1u << 30) || e == 0u) e = 1u;
         ctrl->epoch = e;
         ctrl->ticket[0] = 0u;
+        ctrl->ticket[1] = 0u;
         if (mode == 1) {
             ctrl->status = 0u;
             for (int k = 1; k < 8; ++k) ctrl->ticket[k] = 0u;
             ctrl->count = 0u;
             ctrl->total = 0u;
             ctrl->pair_base = 0u;
+            ctrl->seg_total = 0u;
         }
     }
     if (mode == 1)
@@ -42,10 +44,21 @@ __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t m
     return count ? min(*count, max_count) : max_count;
 }
 
-// Global digit histograms of all passes in one read of the keys.  Per pass, the warp counts
-// the digit of lane 0 with one ballot (the high digits of float depth keys are nearly
-// constant, and same-address shared atomics would serialise) and the other keys with plain
-// shared atomics.
+// Global digit histograms of all passes in one read of the keys (four keys per thread and
+// iteration, 16-byte loads when the keys are 16-byte aligned).  Per pass, the warp counts the
+// digit of lane 0 with one ballot (the high digits of float depth keys are nearly constant, and
+// same-address shared atomics would serialise) and the other keys with plain shared atomics.
+__device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool valid, uint32_t npasses,
+                                         uint32_t lane) {
+    for (uint32_t p = 0; p < npasses; ++p) {
+        const uint32_t d = (k >> (8u * p)) & 255u;
+        const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
+        const uint32_t same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
+        if (lane == 0 && same) atomicAdd(&h[p][d0], (uint32_t)__popc(same));
+        if (valid && d != d0) atomicAdd(&h[p][d], 1u);
+    }
+}
+
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restrict__ keys,
                                                         const uint32_t *count, uint32_t max_count,
                                                         uint32_t npasses, Ctrl *ctrl) {
@@ -55,18 +68,25 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
     const uint32_t n = load_count(count, max_count);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31u;
+    const bool vec = ((uintptr_t)keys & 15u) == 0;
     // Whole warps iterate together (bounds padded to the warp) so the ballots see 32 lanes.
-    const uint32_t nr = (n + 31u) & ~31u;
-    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nr; idx += stride) {
-        const bool valid = idx < n;
-        const uint32_t k = valid ? keys[idx] : 0u;
-        for (uint32_t p = 0; p < npasses; ++p) {
-            const uint32_t d = (k >> (8u * p)) & 255u;
-            const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
-            const uint32_t same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
-            if (lane == 0 && same) atomicAdd(&h[p][d0], (uint32_t)__popc(same));
-            if (valid && d != d0) atomicAdd(&h[p][d], 1u);
+    const uint32_t n4 = (n + 3u) / 4u;
+    const uint32_t nr = (n4 + 31u) & ~31u;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nr; q += stride) {
+        const uint32_t i0 = q * 4u;
+        uint32_t k[4];
+        if (vec && i0 + 4u <= n) {
+            const uint4 v = *reinterpret_cast<const uint4 *>(keys + i0);
+            k[0] = v.x;
+            k[1] = v.y;
+            k[2] = v.z;
+            k[3] = v.w;
+        } else {
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) k[j] = i0 + j < n ? keys[i0 + j] : 0u;
         }
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j) hist_add(h, k[j], i0 + j < n, npasses, lane);
     }
     __syncthreads();
     for (uint32_t p = 0; p < npasses; ++p) {
@@ -333,7 +353,7 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     count_launches(1);
     if (max_count == 0) return cudaGetLastError();
     prof_mark(prof_stage, true, st);
-    uint32_t hist_blocks = (max_count + 256 * 16 - 1) / (256 * 16);
+    uint32_t hist_blocks = (max_count + 256 * 4 * 4 - 1) / (256 * 4 * 4);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
     sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, npasses, L.ctrl);
     count_launches(1);
