@@ -142,7 +142,8 @@ size_t gs_radix_sort_scratch_bytes(uint32_t max_count);
  * kernels src/shader/radix_sort.wgsl:78-529): stable ascending LSD sort of u32 keys carrying
  * u32 values, 8 bits per pass, in place.  The pair count is read from device memory at
  * `count` (e.g. &indirect_args[1]) when non-NULL, else it is `max_count`.  Sorts bits
- * [0, key_bits) (key_bits 1..32; 32 for depth keys).  Bit-exact with a stable sort. */
+ * [0, key_bits) (key_bits 1..32; 32 for depth keys); bits above key_bits are ignored.
+ * Bit-exact with a stable sort by (key mod 2^key_bits). */
 gs_status gs_radix_sort(uint32_t *keys, uint32_t *values, uint32_t max_count,
                         const uint32_t *count, uint32_t key_bits, void *scratch,
                         size_t scratch_bytes, gs_stream stream);

@@ -86,8 +86,9 @@ def test_sort_partial_key_bits(gs, cuda, bits):
     rng = np.random.default_rng(bits)
     n = 70000
     keys = rng.integers(0, 1 << bits, size=n).astype(np.uint32)
+    keys[::3] |= rng.integers(0, 1 << 32, size=keys[::3].size, dtype=np.uint64).astype(np.uint32) & ~np.uint32((1 << bits) - 1)
     vals = np.arange(n, dtype=np.uint32)
-    k, v = _run(gs, cuda, keys, vals, key_bits=bits)
+    k, v = _run(gs, cuda, keys, vals, key_bits=bits)  # bits above key_bits are ignored
     ek, ev = _expect(keys, vals, bits)
     assert np.array_equal(k, ek) and np.array_equal(v, ev)
 

@@ -48,10 +48,11 @@ __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t m
 // iteration, 16-byte loads when the keys are 16-byte aligned).  Per pass, the warp counts the
 // digit of lane 0 with one ballot (the high digits of float depth keys are nearly constant, and
 // same-address shared atomics would serialise) and the other keys with plain shared atomics.
-__device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool valid, uint32_t npasses,
+__device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool valid, uint32_t key_bits,
                                          uint32_t lane) {
-    for (uint32_t p = 0; p < npasses; ++p) {
-        const uint32_t d = (k >> (8u * p)) & 255u;
+    for (uint32_t p = 0; 8u * p < key_bits; ++p) {
+        const uint32_t left = key_bits - 8u * p;
+        const uint32_t d = (k >> (8u * p)) & ((left < 8u ? (1u << left) : 256u) - 1u);
         const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
         const uint32_t same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
         if (lane == 0 && same) atomicAdd(&h[p][d0], (uint32_t)__popc(same));
@@ -61,8 +62,9 @@ __device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool va
 
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restrict__ keys,
                                                         const uint32_t *count, uint32_t max_count,
-                                                        uint32_t npasses, Ctrl *ctrl) {
+                                                        uint32_t key_bits, Ctrl *ctrl) {
     __shared__ uint32_t h[4][256];
+    const uint32_t npasses = (key_bits + 7u) / 8u;
     for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&h[0][0])[k] = 0u;
     __syncthreads();
     const uint32_t n = load_count(count, max_count);
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
             for (uint32_t j = 0; j < 4; ++j) k[j] = i0 + j < n ? keys[i0 + j] : 0u;
         }
 #pragma unroll
-        for (uint32_t j = 0; j < 4; ++j) hist_add(h, k[j], i0 + j < n, npasses, lane);
+        for (uint32_t j = 0; j < 4; ++j) hist_add(h, k[j], i0 + j < n, key_bits, lane);
     }
     __syncthreads();
     for (uint32_t p = 0; p < npasses; ++p) {
@@ -166,7 +168,7 @@ template <bool IN_PACKED, bool OUT_PACKED>
 __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
-    uint32_t max_count, uint32_t pass, Ctrl *ctrl, uint64_t *flags) {
+    uint32_t max_count, uint32_t pass, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags) {
     __shared__ uint2 s_kv[kTileKeys];
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_start[256];
@@ -186,6 +188,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t tile = s_tile, epoch = s_epoch;
     if (tile >= ntiles) return;
     const uint32_t shift = 8u * pass;
+    const uint32_t dmask = (1u << digit_bits) - 1u;  // bits above the key width are ignored
     const uint32_t base = tile * kTileKeys + warp * (32u * kSortRows);
 
     uint32_t k[kSortRows], r[kSortRows];
@@ -206,10 +209,11 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (uint32_t i = 0; i < kSortRows; ++i) {
-        const uint32_t d = (k[i] >> shift) & 255u;
+        const uint32_t d = (k[i] >> shift) & dmask;
         uint32_t peers = 0xFFFFFFFFu;
 #pragma unroll
         for (uint32_t b = 0; b < 8; ++b) {
+            if (b >= digit_bits) break;  // bits above the key width are zero in every key
             const uint32_t bit = (d >> b) & 1u;
             const uint32_t bal = __ballot_sync(0xFFFFFFFFu, bit);
             peers &= bit ? bal : ~bal;
@@ -234,7 +238,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     }
     const uint32_t total = run;
     const uint32_t invalid = (tile == ntiles - 1) ? ntiles * kTileKeys - n : 0u;
-    const uint32_t pub = (d == 255u) ? total - invalid : total;
+    // Padding keys (all ones) rank last, in the largest digit.
+    const uint32_t pub = (d == dmask) ? total - invalid : total;
     uint64_t *f = flags + (size_t)tile * 256u + d;
     st_relaxed(f, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
 
@@ -253,7 +258,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     if constexpr (IN_PACKED) {
 #pragma unroll
         for (uint32_t i = 0; i < kSortRows; ++i) {
-            const uint32_t dd = (k[i] >> shift) & 255u;
+            const uint32_t dd = (k[i] >> shift) & dmask;
             s_kv[s_start[dd] + s_whist[warp][dd] + r[i]] = make_uint2(k[i], v[i]);
         }
     } else {
@@ -262,7 +267,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
         for (uint32_t i = 0; i < kSortRows; ++i) {
             const uint32_t pos = base + i * 32u + lane;
             const uint32_t vv = pos < n ? vin[pos] : 0u;
-            const uint32_t dd = (k[i] >> shift) & 255u;
+            const uint32_t dd = (k[i] >> shift) & dmask;
             s_kv[s_start[dd] + s_whist[warp][dd] + r[i]] = make_uint2(k[i], vv);
         }
     }
@@ -270,7 +275,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t valid = min(kTileKeys, n - tile * kTileKeys);
     for (uint32_t j = tid; j < valid; j += kSortThreads) {
         const uint2 kv = s_kv[j];
-        const uint32_t dd = (kv.x >> shift) & 255u;
+        const uint32_t dd = (kv.x >> shift) & dmask;
         const uint32_t o = s_gbase[dd] + (j - s_start[dd]);
         if (o < n) {  // always true unless a look-back timed out (status already set)
             if constexpr (OUT_PACKED) {
@@ -299,6 +304,12 @@ __global__ void copy_packed_kernel(const uint2 *src, uint2 *dst, const uint32_t 
 }
 
 static inline uint32_t sort_passes(uint32_t key_bits) { return (key_bits + 7u) / 8u; }
+// Live bits of pass p's digit: keys are below 2^key_bits.  Invalid (padding) keys are all ones
+// but sort last either way, because they hold the largest value in every live bit.
+static inline uint32_t pass_bits(uint32_t key_bits, uint32_t p) {
+    const uint32_t left = key_bits - 8u * p;
+    return left < 8u ? left : 8u;
+}
 
 struct SortLayout {
     Ctrl *ctrl;
@@ -355,27 +366,30 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     prof_mark(prof_stage, true, st);
     uint32_t hist_blocks = (max_count + 256 * 4 * 4 - 1) / (256 * 4 * 4);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
-    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, npasses, L.ctrl);
+    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, key_bits, L.ctrl);
     count_launches(1);
     const size_t fstride = (size_t)L.ntiles * 256;
     if (npasses == 1) {
         sort_pass_kernel<false, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, L.alt_a,
-                                                                        count, max_count, 0, L.ctrl, L.flags);
+                                                                        count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
         unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
         count_launches(2);
     } else {
         uint2 *src = L.alt_a, *dst = L.alt_b;
         sort_pass_kernel<false, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, src,
-                                                                        count, max_count, 0, L.ctrl, L.flags);
+                                                                        count, max_count, 0, pass_bits(key_bits, 0),
+                                                                        L.ctrl, L.flags);
         for (uint32_t p = 1; p + 1 < npasses; ++p) {
             sort_pass_kernel<true, true><<<L.ntiles, kSortThreads, 0, st>>>(
-                nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, L.ctrl, L.flags + p * fstride);
+                nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, pass_bits(key_bits, p), L.ctrl,
+                L.flags + p * fstride);
             uint2 *t = src;
             src = dst;
             dst = t;
         }
         sort_pass_kernel<true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, keys, vals, nullptr, count,
-                                                                        max_count, npasses - 1, L.ctrl,
+                                                                        max_count, npasses - 1,
+                                                                        pass_bits(key_bits, npasses - 1), L.ctrl,
                                                                         L.flags + (npasses - 1) * fstride);
         count_launches(npasses);
     }
@@ -400,7 +414,8 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
     uint2 *src = data, *dst = L.alt_a;
     for (uint32_t p = 0; p < npasses; ++p) {
         sort_pass_kernel<true, true><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
-                                                                       count, max_count, p, L.ctrl, L.flags + p * fstride);
+                                                                       count, max_count, p, pass_bits(key_bits, p), L.ctrl,
+                                                                       L.flags + p * fstride);
         uint2 *t = src;
         src = dst;
         dst = t;
