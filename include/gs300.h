@@ -148,6 +148,20 @@ gs_status gs_radix_sort(uint32_t *keys, uint32_t *values, uint32_t max_count,
                         const uint32_t *count, uint32_t key_bits, void *scratch,
                         size_t scratch_bytes, gs_stream stream);
 
+/* Allocation-free variant of gs_radix_sort (no counterpart in the reference, whose sorter always
+ * owns its buffers).  For callers that must not call cudaMalloc: a frame loop that may not
+ * allocate or synchronise mid-frame, or a host runtime whose device memory belongs to another
+ * allocator and that therefore cannot hand this library a scratch buffer.  Same contract as
+ * gs_radix_sort (stable, in place, bits [0, key_bits), device-side `count`), but its scratch is a
+ * static device array inside the library: at most 1,048,576 (2^20) pairs per call, and every
+ * device that loads the library holds about 19 MB for it until the process exits.  Larger
+ * `max_count` returns GS_ERR_INVALID_ARG.  The first call on a device looks up the array's device
+ * address and clears it on `stream`; make that first call before any stream capture.  All calls
+ * share the one array, so calls whose work overlaps on the GPU (different streams, no ordering
+ * between them) race: order them on one stream or synchronise between them. */
+gs_status gs_radix_sort_no_alloc(uint32_t *keys, uint32_t *values, uint32_t max_count,
+                                 const uint32_t *count, uint32_t key_bits, gs_stream stream);
+
 /* Bytes of scratch gs_rasterize needs for up to `max_splats` visible splats, a
  * width x height target and up to `max_pairs` (tile, splat) pairs. */
 size_t gs_rasterize_scratch_bytes(uint32_t max_splats, uint32_t width, uint32_t height,

@@ -261,6 +261,8 @@ gs_status check_target(const uint8_t *target, uint32_t w, uint32_t h, uint32_t p
 
 // ---- stage timers and launch counter ---------------------------------------------------------
 namespace gs {
+gs_status set_error(gs_status status, const char *message) { return fail(status, "%s", message); }
+
 namespace {
 std::atomic<uint64_t> g_launches{0};
 std::mutex g_prof_mu;

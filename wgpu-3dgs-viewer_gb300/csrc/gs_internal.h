@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "gs_common.cuh"
+#include "gs300.h"
 #include "gs_record.h"
 
 namespace gs {
@@ -16,6 +17,9 @@ namespace gs {
 enum ProfStage { kProfPreprocess = 0, kProfDepthSort, kProfBin, kProfTileSort, kProfRanges, kProfRaster, kProfStages };
 void prof_mark(int stage, bool begin, cudaStream_t st);
 void count_launches(uint32_t n);
+
+// Records `message` as the calling thread's gs_last_error() and returns `status`.
+gs_status set_error(gs_status status, const char *message);
 
 // Resets a control block: mode 1 = a new stage call (epoch, status, tickets, counters,
 // histograms); mode 0 = a new segment inside a call (epoch and ticket[0] only).

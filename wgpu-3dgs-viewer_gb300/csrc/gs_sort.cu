@@ -9,6 +9,9 @@
 // then scatters through shared memory so that each digit's run is written contiguously.
 // The key count may live in device memory (the preprocess instance count), so a whole frame
 // can be enqueued (or graph-captured) without a host round trip.
+#include <mutex>
+
+#include "gs300.h"
 #include "gs_internal.h"
 
 namespace gs {
@@ -428,4 +431,59 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
     return cudaGetLastError();
 }
 
+// ---- allocation-free sort entry point -------------------------------------------------------
+// Scratch for gs_radix_sort_no_alloc lives in this file-scope device array instead of memory the
+// caller provides, so that entry point never allocates.  It is sized for kNoAllocMaxPairs pairs
+// of 32-bit keys (the 4-pass layout of sort_scratch_bytes) and every device that loads the
+// library holds it until the process exits.
+constexpr uint32_t kNoAllocMaxPairs = 1u << 20;
+constexpr size_t kNoAllocTiles = (kNoAllocMaxPairs + kTileKeys - 1) / kTileKeys;
+constexpr size_t kNoAllocBytes = ((sizeof(Ctrl) + 255) / 256) * 256 + 2 * (((size_t)kNoAllocMaxPairs * 8 + 255) / 256) * 256 +
+                                 4 * kNoAllocTiles * 256 * sizeof(uint64_t);
+static __device__ __align__(256) unsigned char g_no_alloc_scratch[kNoAllocBytes];
+
+namespace {
+std::mutex g_no_alloc_mu;
+constexpr int kNoAllocDevices = 64;
+void *g_no_alloc_ptr[kNoAllocDevices] = {};
+}  // namespace
+
+// Device address of the array on the current device.  The first call on a device looks the
+// address up (in host code the array's name is only a stand-in, not a device address) and clears
+// the array on `st`; later calls reuse the cached address.
+static cudaError_t no_alloc_scratch(void **out, cudaStream_t st) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(g_no_alloc_mu);
+    if (!g_no_alloc_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_no_alloc_scratch);
+        if (e != cudaSuccess) return e;
+        e = cudaMemsetAsync(p, 0, kNoAllocBytes, st);
+        if (e != cudaSuccess) return e;
+        g_no_alloc_ptr[dev] = p;
+    }
+    *out = g_no_alloc_ptr[dev];
+    return cudaSuccess;
+}
+
 }  // namespace gs
+
+extern "C" gs_status gs_radix_sort_no_alloc(uint32_t *keys, uint32_t *values, uint32_t max_count,
+                                            const uint32_t *count, uint32_t key_bits, gs_stream stream) {
+    using namespace gs;
+    if (key_bits < 1 || key_bits > 32) return set_error(GS_ERR_INVALID_ARG, "gs_radix_sort_no_alloc: key_bits not in 1..=32");
+    if (max_count > kNoAllocMaxPairs)
+        return set_error(GS_ERR_INVALID_ARG,
+                         "gs_radix_sort_no_alloc: max_count exceeds the static scratch limit of 1048576 pairs "
+                         "(use gs_radix_sort with caller scratch)");
+    if (max_count && (!keys || !values)) return set_error(GS_ERR_INVALID_ARG, "gs_radix_sort_no_alloc: NULL buffer");
+    cudaStream_t st = (cudaStream_t)stream;
+    void *scratch = nullptr;
+    cudaError_t e = no_alloc_scratch(&scratch, st);
+    if (e == cudaSuccess) e = launch_sort(keys, values, max_count, count, key_bits, scratch, st);
+    if (e != cudaSuccess) return set_error(GS_ERR_CUDA, cudaGetErrorString(e));
+    return GS_OK;
+}

@@ -57,6 +57,7 @@ SIGNATURES = [
     ("gs_preprocess", ST, [P, P, U32, U32, P, I32, P, P, P, P, U32, P, P, SZ, P]),
     ("gs_radix_sort_scratch_bytes", SZ, [U32]),
     ("gs_radix_sort", ST, [P, P, U32, P, U32, P, SZ, P]),
+    ("gs_radix_sort_no_alloc", ST, [P, P, U32, P, U32, P]),
     ("gs_rasterize_scratch_bytes", SZ, [U32, U32, U32, U32]),
     ("gs_rasterize", ST, [P, P, P, P, U32, P, U32, U32, U32, U32, P, SZ, P]),
     ("gs_scratch_status", ST, [P, P, ctypes.POINTER(U32)]),
