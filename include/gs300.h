@@ -57,6 +57,10 @@ uint64_t gs_launch_count(void);
 gs_status gs_profile_enable(int enable);
 /* Synchronises the device; ms[s] = summed stage time, launches[s] = timed launches. */
 gs_status gs_profile_read(double ms[GS_PROF_STAGES], uint32_t launches[GS_PROF_STAGES]);
+/* While profiling, splat-mode frames use a counting rasteriser; this returns its tallies since
+ * gs_profile_enable (synchronises): pixel-splat evaluations, fragment alphas, channel-triple
+ * blends, transmittance updates. */
+gs_status gs_profile_counters(uint64_t out[4]);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Host-side helpers (no device work).                                                         */

@@ -277,6 +277,8 @@ StageEvents g_prof[kProfStages];
 
 void count_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+bool prof_enabled() { return g_prof_on; }
+
 void prof_mark(int stage, bool begin, cudaStream_t st) {
     if (!g_prof_on) return;
     std::lock_guard<std::mutex> g(g_prof_mu);
@@ -306,7 +308,18 @@ const char *gs_version(void) { return "gs300 0.1.0 sm_103a"; }
 
 uint64_t gs_launch_count(void) { return gs::g_launches.load(); }
 
+gs_status gs_profile_counters(uint64_t out[4]) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    GS_CUDA(cudaDeviceSynchronize());
+    unsigned long long c[4];
+    GS_CUDA(gs::raster_counters(c, false));
+    for (int i = 0; i < 4; ++i) out[i] = c[i];
+    return GS_OK;
+}
+
 gs_status gs_profile_enable(int enable) {
+    unsigned long long discard[4];
+    GS_CUDA(gs::raster_counters(discard, true));
     std::lock_guard<std::mutex> g(gs::g_prof_mu);
     for (auto &e : gs::g_prof) {
         e.used = 0;

@@ -16,6 +16,10 @@ namespace gs {
 // the count of kernels this library has launched.
 enum ProfStage { kProfPreprocess = 0, kProfDepthSort, kProfBin, kProfTileSort, kProfRanges, kProfRaster, kProfStages };
 void prof_mark(int stage, bool begin, cudaStream_t st);
+bool prof_enabled();
+// Work tallies of the counting rasteriser run while profiling: pixel-splat evaluations,
+// alphas, channel-triple blends, transmittance updates.
+cudaError_t raster_counters(unsigned long long out[4], bool reset);
 void count_launches(uint32_t n);
 
 // Records `message` as the calling thread's gs_last_error() and returns `status`.

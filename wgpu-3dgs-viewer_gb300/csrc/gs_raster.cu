@@ -494,12 +494,15 @@ __device__ __forceinline__ uint32_t compact_chunk(RasterShared &S, uint32_t cnt,
 //      whose bounds do not meet restarts B from k - (n - k) (k = 0 starts from the cleared
 //      value, which is exact).
 // Every pixel therefore ends bit-identical to the full back-to-front pass.
-template <uint32_t MODE, bool PORTABLE_EXP>
+template <uint32_t MODE, bool PORTABLE_EXP, bool COUNT>
 __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
     const gs_splat *__restrict__ sorted, const uint2 *__restrict__ pairs, const uint2 *__restrict__ ranges,
     uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch, uint32_t tiles_x, float std2,
-    float outline2, uint32_t max_splats, uint32_t suffix_min, float eps) {
+    float outline2, uint32_t max_splats, uint32_t suffix_min, float eps, unsigned long long *counters) {
     __shared__ RasterShared S;
+    // Work tallies of the counting variant (profiling only): fragment evaluations, alphas,
+    // channel-triple blends and transmittance updates.
+    uint32_t n_eval = 0, n_alpha = 0, n_blend = 0, n_trans = 0;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
     const uint2 range = ranges[blockIdx.x];
@@ -520,7 +523,9 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
             for (uint32_t i = 0; i < nl; ++i) {
                 const uint32_t j = S.list[warp][i];
                 float al;
+                if (COUNT) ++n_eval;
                 if (!fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) continue;
+                if (COUNT) ++n_alpha, ++n_blend;
                 const float4 c = S.c[j];
                 const float om = __fsub_rn(1.0f, al);
                 d0 = blend8(d0, om, __fmul_rn(c.x, al));
@@ -545,7 +550,9 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
                     if (__all_sync(0xFFFFFFFFu, found)) break;
                     const uint32_t j = S.list[warp][i];
                     float al;
+                    if (COUNT && !found) ++n_eval;
                     if (!found && fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) {
+                        if (COUNT) ++n_alpha, ++n_trans;
                         T = __fmul_rn(T, __fsub_rn(1.0f, al));
                         if (T < eps) {
                             found = true;
@@ -590,7 +597,9 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
                             const uint32_t j = S.list[warp][i];
                             float al;
                             if (!inside) continue;
+                            if (COUNT) ++n_eval;
                             if (!fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) continue;
+                            if (COUNT) ++n_alpha, ++n_blend;
                             const float4 c = S.c[j];
                             const float om = __fsub_rn(1.0f, al);
                             d0 = blend8(d0, om, __fmul_rn(c.x, al));
@@ -607,7 +616,9 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
                             const uint32_t j = S.list[warp][i];
                             float al;
                             if (!active || base + j < k) continue;
+                            if (COUNT) ++n_eval;
                             if (!fragment<MODE, PORTABLE_EXP>(S.a[j], S.b[j], pxc, pyc, outline2, &al)) continue;
+                            if (COUNT) ++n_alpha, n_blend += 2;
                             const float4 c = S.c[j];
                             const float om = __fsub_rn(1.0f, al);
                             const float s0a = __fmul_rn(c.x, al), s1a = __fmul_rn(c.y, al), s2a = __fmul_rn(c.z, al);
@@ -636,6 +647,26 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
         const uint32_t rgba = (uint32_t)d0 | ((uint32_t)d1 << 8) | ((uint32_t)d2 << 16) | 0xFF000000u;
         *reinterpret_cast<uint32_t *>(target + (size_t)py * pitch + (size_t)px * 4u) = rgba;
     }
+    if constexpr (COUNT) {
+        const uint32_t v[4] = {n_eval, n_alpha, n_blend, n_trans};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const uint32_t w = __reduce_add_sync(0xFFFFFFFFu, v[q]);
+            if (lane == 0 && w) atomicAdd(counters + q, (unsigned long long)w);
+        }
+    }
+}
+
+// Work tallies of the counting raster variant (profiling only).
+static __device__ unsigned long long g_raster_counts[4];
+
+cudaError_t raster_counters(unsigned long long out[4], bool reset) {
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_raster_counts, sizeof(g_raster_counts));
+    if (e == cudaSuccess && reset) {
+        const unsigned long long zero[4] = {0, 0, 0, 0};
+        e = cudaMemcpyToSymbol(g_raster_counts, zero, sizeof(zero));
+    }
+    return e;
 }
 
 template <uint32_t MODE>
@@ -643,12 +674,21 @@ static void launch_raster_mode(const RasterLayout &L, const gs_splat *splats, ui
                                uint32_t pitch, float std2, float outline2, int exact, uint32_t max_splats,
                                cudaStream_t st) {
     const RasterTuning t = raster_tuning();
-    if (exact)
-        raster_kernel<MODE, true><<<L.ntiles, kRasterThreads, 0, st>>>(
-            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
-    else
-        raster_kernel<MODE, false><<<L.ntiles, kRasterThreads, 0, st>>>(
-            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps);
+    if (exact) {
+        raster_kernel<MODE, true, false><<<L.ntiles, kRasterThreads, 0, st>>>(
+            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
+            nullptr);
+    } else if (MODE == GS_DISPLAY_SPLAT && prof_enabled()) {
+        unsigned long long *counts = nullptr;
+        cudaGetSymbolAddress((void **)&counts, g_raster_counts);
+        raster_kernel<GS_DISPLAY_SPLAT, false, true><<<L.ntiles, kRasterThreads, 0, st>>>(
+            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
+            counts);
+    } else {
+        raster_kernel<MODE, false, false><<<L.ntiles, kRasterThreads, 0, st>>>(
+            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
+            nullptr);
+    }
 }
 
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,

@@ -66,6 +66,13 @@ def profile_read():
     return {s: (ms[i], n[i]) for i, s in enumerate(PROFILE_STAGES)}
 
 
+def profile_counters():
+    """Rasteriser work tallies since profile_enable: evaluations, alphas, blends, transmittance."""
+    out = (ctypes.c_uint64 * 4)()
+    check(lib().gs_profile_counters(ref(out)))
+    return {"evaluations": out[0], "alphas": out[1], "blends": out[2], "transmittance": out[3]}
+
+
 def _stream(stream):
     if stream is None:
         return None

@@ -45,6 +45,7 @@ SIGNATURES = [
     ("gs_launch_count", ctypes.c_uint64, []),
     ("gs_profile_enable", ST, [I32]),
     ("gs_profile_read", ST, [P, P]),
+    ("gs_profile_counters", ST, [P]),
     ("gs_camera_view", ST, [P, P]),
     ("gs_camera_projection", ST, [P, F32, P]),
     ("gs_camera_pod_new", ST, [P, U32, U32, P]),
