@@ -286,6 +286,61 @@ gs_status gs_multi_viewer_render(gs_multi_viewer *viewer, const char *const *key
                                  uint32_t height, uint32_t pitch_bytes, gs_stream stream);
 gs_status gs_multi_viewer_synchronize(gs_multi_viewer *viewer, gs_stream stream);
 
+/* ------------------------------------------------------------------------------------------ */
+/* Batches (no counterpart in the reference): many views, each one model of a MultiModelViewer */
+/* seen by its own camera into its own RGBA8 target, rendered by one CUDA graph per batch     */
+/* shape.  A shape is the list of (model, target size, target pointer, pitch) plus the        */
+/* viewer's GaussianTransform; cameras and model transforms may change between calls (they    */
+/* reach the graph through a device uniform buffer).  Views run concurrently on the device.   */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct gs_batch gs_batch;
+typedef struct gs_batch_view {
+    uint32_t model; /* index into the keys given to gs_batch_create */
+    uint32_t width, height, pitch;
+    uint8_t *target;
+    gs_camera_pod camera;
+} gs_batch_view;
+gs_status gs_batch_create(gs_multi_viewer *viewer, const char *const *keys, uint32_t key_count,
+                          gs_batch **out_batch);
+void gs_batch_destroy(gs_batch *batch);
+/* Enqueue all views on `stream` (asynchronous); models missing from the viewer give
+ * GS_ERR_NOT_FOUND and nothing is rendered. */
+gs_status gs_batch_render(gs_batch *batch, const gs_batch_view *views, uint32_t view_count,
+                          gs_stream stream);
+/* Wait, check every view's device status, regrow overflowed tile-pair lists and re-render. */
+gs_status gs_batch_synchronize(gs_batch *batch, gs_stream stream);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Serving (no counterpart in the reference): scenes stay resident (the models of a           */
+/* MultiModelViewer); (scene, camera, resolution) requests are admitted first come first      */
+/* served while the device memory their per-view buffers need fits `budget_bytes` and one of  */
+/* `max_inflight` slots is free; each admitted request runs on its own stream, so requests     */
+/* that arrive while others run overlap with them.  A scheduler thread owns all submission.   */
+/* Models must stay in the viewer while requests for them are queued or running.              */
+/* ------------------------------------------------------------------------------------------ */
+typedef struct gs_server gs_server;
+typedef struct gs_server_report {
+    uint64_t completed, failed;
+    uint32_t queued, running;
+    uint64_t reserved_bytes;
+    double p50_ms, p99_ms, mean_ms, max_ms; /* submit-to-completion latency */
+} gs_server_report;
+gs_status gs_server_create(gs_multi_viewer *viewer, size_t budget_bytes, uint32_t max_inflight,
+                           gs_server **out_server);
+void gs_server_destroy(gs_server *server);
+/* Device bytes a request for a scene of `n` Gaussians at width x height holds while admitted. */
+size_t gs_server_request_bytes(uint32_t n, uint32_t width, uint32_t height);
+/* Queue a request.  `out` (nullable): a device RGBA8 buffer with `out_pitch`, or with
+ * out_on_host != 0 a host buffer of width*height*4 bytes filled when the request completes.
+ * GS_ERR_ADMISSION if the request alone exceeds the budget. */
+gs_status gs_server_submit(gs_server *server, const char *key, const gs_camera_pod *camera,
+                           uint32_t width, uint32_t height, uint8_t *out, uint32_t out_pitch,
+                           int out_on_host, uint64_t *ticket);
+/* Wait for a request (host-side timeout in seconds); reports its latency. */
+gs_status gs_server_wait(gs_server *server, uint64_t ticket, double timeout_s, double *latency_ms);
+gs_status gs_server_stats(gs_server *server, gs_server_report *out);
+gs_status gs_server_reset_stats(gs_server *server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -2,6 +2,7 @@
 
 Flags: -ffp-contract=off so every FP32 multiply and add rounds on its own (the evaluation
 order the CUDA kernels reproduce with -fmad=false); OpenMP for the CPU-baseline leg.
+gs_oracle64.cpp is the FP64 twin used as the precision tier's error reference.
 """
 import os
 import subprocess
@@ -11,18 +12,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgs_oracle.so")
-SRC = os.path.join(HERE, "gs_oracle.cpp")
+SRCS = [os.path.join(HERE, "gs_oracle.cpp"), os.path.join(HERE, "gs_oracle64.cpp")]
 
 
 def build(force=False, verbose=False):
     os.makedirs(OUT_DIR, exist_ok=True)
-    deps = [SRC, os.path.join(ROOT, "include", "gs_record.h")]
+    deps = SRCS + [os.path.join(ROOT, "include", "gs_record.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = [
         "g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-        "-Wall", "-I", os.path.join(ROOT, "include"), SRC, "-o", tmp,
+        "-Wall", "-I", os.path.join(ROOT, "include"), *SRCS, "-o", tmp,
     ]
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

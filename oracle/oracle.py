@@ -38,6 +38,8 @@ def _declare(L):
     L.oracle_exp_portable.restype = ctypes.c_float
     L.oracle_render.argtypes = [P, P, U, U, P, P, P, P, U, U, I, I, I]
     L.oracle_render.restype = U
+    L.oracle64_render.argtypes = [P, P, P, P, U, U, P, U, U, I]
+    L.oracle64_render.restype = U
 
 
 def _p(a):
@@ -118,6 +120,14 @@ def render(u, records, fmt, w, h, exp_mode=0, threads=0, target=None):
         target = np.empty((h, w, 4), np.uint8)
     v = lib().oracle_render(_p(u), _p(records), fmt, n, _p(idx), _p(dep), _p(spl), _p(target), w, h, exp_mode, threads, clear)
     return target, idx[:v].copy(), dep[:v].copy(), spl[:n]
+
+
+def render64(camera_pod, model_pod, gt_pod, records, fmt, w, h, threads=0):
+    """The same frame evaluated in FP64 from the same pods and records (precision reference)."""
+    img = np.empty((h, w, 4), np.uint8)
+    v = lib().oracle64_render(_p(camera_pod), _p(model_pod), _p(gt_pod), _p(records), fmt, len(records), _p(img), w, h,
+                              threads or nproc())
+    return img, v
 
 
 def exp_portable(x):

@@ -103,3 +103,17 @@ def test_half_records_close_to_fp32(oracle, fmt):
     mse = (d.astype(np.float64) ** 2).mean()
     psnr = 10 * math.log10(255.0 ** 2 / max(mse, 1e-12))
     assert psnr > 35.0
+
+
+def test_fp64_twin_agrees_with_fp32_oracle(oracle):
+    """The FP64 twin (precision reference) and the FP32 oracle differ by rounding only."""
+    n, w, h = 30000, 320, 180
+    sc = S.synth_scene(n, seed=8)
+    pod = oracle.camera_pod(S.orbit_camera(4), w, h)
+    mt, gt = R.ModelTransformPod.new(), R.GaussianTransformPod.new()
+    u = oracle.frame_uniforms(pod, mt, gt, w, h)
+    a, *_ = oracle.render(u, sc, R.FORMAT_FP32, w, h, exp_mode=1, threads=4)
+    b, v = oracle.render64(pod, mt, gt, sc, R.FORMAT_FP32, w, h, threads=4)
+    d = np.abs(a.astype(np.int32) - b.astype(np.int32))[..., :3]
+    mse = (d.astype(np.float64) ** 2).mean()
+    assert v > n // 2 and d.max() <= 2 and 10 * math.log10(255.0 ** 2 / max(mse, 1e-12)) > 60.0

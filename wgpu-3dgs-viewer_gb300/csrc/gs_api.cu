@@ -8,8 +8,14 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <map>
+#include <thread>
+#include <unordered_map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -275,12 +281,20 @@ struct StageEvents {
 StageEvents g_prof[kProfStages];
 }  // namespace
 
-void count_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+// While a batch graph is being captured on this thread, launches are counted into the graph
+// (and charged on every replay) and stage timers are off.
+thread_local bool t_capturing = false;
+thread_local uint64_t t_captured_launches = 0;
+
+void count_launches(uint32_t n) {
+    if (t_capturing) t_captured_launches += n;
+    else g_launches.fetch_add(n, std::memory_order_relaxed);
+}
 
 bool prof_enabled() { return g_prof_on; }
 
 void prof_mark(int stage, bool begin, cudaStream_t st) {
-    if (!g_prof_on) return;
+    if (!g_prof_on || t_capturing) return;
     std::lock_guard<std::mutex> g(g_prof_mu);
     StageEvents &e = g_prof[stage];
     if (begin) {
@@ -945,5 +959,536 @@ gs_status gs_multi_viewer_synchronize(gs_multi_viewer *v, gs_stream stream) {
     }
     return fail(GS_ERR_CAPACITY, "tile-pair list kept overflowing");
 }
+
+}  // extern "C"
+
+namespace {
+
+// ---- Batches: many views (model, camera, target) rendered by one CUDA graph ------------------
+struct ViewSlot {
+    const Model *model = nullptr;
+    uint32_t w = 0, h = 0;
+    DevBuf control, indices, depths, splats, pre_scratch, sort_scratch, raster_scratch;
+    uint32_t max_pairs = 0, raster_n = 0, raster_w = 0, raster_h = 0;
+
+    // Buffers of one view of `m` at w x h; returns true when anything was (re)allocated.
+    cudaError_t prepare(const Model *m, uint32_t ww, uint32_t hh, bool *changed) {
+        const uint32_t n = m->n;
+        cudaError_t e = cudaSuccess;
+        if (model == nullptr || model->n != n) {
+            if ((e = control.ensure(64)) != cudaSuccess) return e;
+            if ((e = cudaMemset(control.ptr, 0, 64)) != cudaSuccess) return e;
+            if ((e = indices.ensure((size_t)n * 4)) != cudaSuccess) return e;
+            if ((e = depths.ensure((size_t)gs_depth_capacity(n) * 4)) != cudaSuccess) return e;
+            if ((e = splats.ensure((size_t)n * sizeof(gs_splat))) != cudaSuccess) return e;
+            if ((e = pre_scratch.ensure(preprocess_scratch_bytes(n))) != cudaSuccess) return e;
+            if ((e = cudaMemset(pre_scratch.ptr, 0, pre_scratch.bytes)) != cudaSuccess) return e;
+            if ((e = sort_scratch.ensure(sort_scratch_bytes(n, 32))) != cudaSuccess) return e;
+            if ((e = cudaMemset(sort_scratch.ptr, 0, sort_scratch.bytes)) != cudaSuccess) return e;
+            *changed = true;
+        }
+        if (max_pairs == 0) max_pairs = default_pairs(n, ww, hh);
+        if (!raster_scratch.ptr || raster_n < n || raster_w != ww || raster_h != hh) {
+            const size_t b = raster_scratch_bytes(n, ww, hh, max_pairs);
+            raster_scratch.release();
+            if ((e = raster_scratch.ensure(b)) != cudaSuccess) return e;
+            if ((e = cudaMemset(raster_scratch.ptr, 0, b)) != cudaSuccess) return e;
+            raster_n = n;
+            raster_w = ww;
+            raster_h = hh;
+            *changed = true;
+        }
+        model = m;
+        w = ww;
+        h = hh;
+        return cudaSuccess;
+    }
+};
+
+}  // namespace
+
+struct gs_batch {
+    gs_multi_viewer *mv = nullptr;
+    std::vector<std::string> keys;
+    std::vector<ViewSlot> slots;
+    DevBuf uniforms_dev;
+    gs_frame_uniforms *uniforms_host = nullptr;  // pinned, one per view
+    uint32_t uniforms_cap = 0;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    cudaStream_t capture = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::string shape;
+    uint64_t graph_launches = 0;
+    std::vector<gs_batch_view> last;
+    std::mutex mu;
+
+    ~gs_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (auto s : streams) cudaStreamDestroy(s);
+        for (auto e : events) cudaEventDestroy(e);
+        if (capture) cudaStreamDestroy(capture);
+        if (uniforms_host) cudaFreeHost(uniforms_host);
+    }
+};
+
+namespace {
+
+constexpr uint32_t kBatchStreams = 16;
+
+gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t n, cudaStream_t st) {
+    gs_multi_viewer *mv = b->mv;
+    std::lock_guard<std::mutex> g(mv->mu);
+    if (n == 0) return GS_OK;
+    std::vector<const Model *> ms(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (views[i].model >= b->keys.size()) return fail(GS_ERR_INVALID_ARG, "view %u: model index %u out of range", i, views[i].model);
+        auto it = mv->models.find(b->keys[views[i].model]);
+        if (it == mv->models.end()) return fail(GS_ERR_NOT_FOUND, "model '%s' not found", b->keys[views[i].model].c_str());
+        ms[i] = it->second;
+        const gs_status s = check_target(views[i].target, views[i].width, views[i].height, views[i].pitch);
+        if (s != GS_OK) return s;
+    }
+    if (n > b->uniforms_cap) {
+        if (b->uniforms_host) cudaFreeHost(b->uniforms_host);
+        b->uniforms_host = nullptr;
+        GS_CUDA(cudaMallocHost(&b->uniforms_host, (size_t)n * sizeof(gs_frame_uniforms)));
+        GS_CUDA(b->uniforms_dev.ensure((size_t)n * sizeof(gs_frame_uniforms)));
+        b->uniforms_cap = n;
+    }
+    if (b->slots.size() < n) b->slots.resize(n);
+    bool changed = false;
+    std::string shape(reinterpret_cast<const char *>(&mv->frame.gt), sizeof(gs_gaussian_transform_pod));
+    for (uint32_t i = 0; i < n; ++i) {
+        GS_CUDA(b->slots[i].prepare(ms[i], views[i].width, views[i].height, &changed));
+        const gs_status s = gs_frame_uniforms_build(&views[i].camera, &ms[i]->model, &mv->frame.gt, views[i].width,
+                                                    views[i].height, &b->uniforms_host[i]);
+        if (s != GS_OK) return s;
+        const uintptr_t key[7] = {(uintptr_t)ms[i], ms[i]->n, views[i].width, views[i].height, views[i].pitch,
+                                  (uintptr_t)views[i].target, (uintptr_t)ms[i]->has_selection};
+        shape.append(reinterpret_cast<const char *>(key), sizeof(key));
+    }
+    if (changed || shape != b->shape || !b->exec) {
+        if (b->exec) cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        if (!b->capture) GS_CUDA(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking));
+        while (b->streams.size() < kBatchStreams) {
+            cudaStream_t s;
+            GS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            b->streams.push_back(s);
+        }
+        while (b->events.size() < kBatchStreams + 1) {
+            cudaEvent_t e;
+            GS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            b->events.push_back(e);
+        }
+        const uint32_t nstreams = n < kBatchStreams ? n : kBatchStreams;
+        GS_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
+        t_capturing = true;
+        t_captured_launches = 0;
+        cudaError_t err = cudaEventRecord(b->events[kBatchStreams], b->capture);
+        for (uint32_t s = 0; s < nstreams && err == cudaSuccess; ++s)
+            err = cudaStreamWaitEvent(b->streams[s], b->events[kBatchStreams], 0);
+        const gs_frame_uniforms *udev = reinterpret_cast<const gs_frame_uniforms *>(b->uniforms_dev.ptr);
+        for (uint32_t i = 0; i < n && err == cudaSuccess; ++i) {
+            ViewSlot &v = b->slots[i];
+            const Model *m = ms[i];
+            cudaStream_t vs = b->streams[i % nstreams];
+            uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+            err = launch_preprocess(b->uniforms_host[i], m->records.ptr, m->format, m->n,
+                                    m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert, ind,
+                                    ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr, gs_depth_capacity(m->n),
+                                    (gs_splat *)v.splats.ptr, v.pre_scratch.ptr, vs, udev + i);
+            if (err == cudaSuccess)
+                err = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, 32,
+                                  v.sort_scratch.ptr, vs);
+            if (err == cudaSuccess) {
+                const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
+                err = launch_raster(&seg, 1, b->uniforms_host[i], views[i].target, views[i].width, views[i].height,
+                                    views[i].pitch, v.max_pairs, v.raster_scratch.ptr, mv->frame.exact_exp, vs);
+            }
+        }
+        for (uint32_t s = 0; s < nstreams && err == cudaSuccess; ++s) {
+            err = cudaEventRecord(b->events[s], b->streams[s]);
+            if (err == cudaSuccess) err = cudaStreamWaitEvent(b->capture, b->events[s], 0);
+        }
+        t_capturing = false;
+        cudaGraph_t graph = nullptr;
+        const cudaError_t end = cudaStreamEndCapture(b->capture, &graph);
+        if (err == cudaSuccess) err = end;
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&b->exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (err != cudaSuccess) return cuda_fail(err, "batch graph capture");
+        b->graph_launches = t_captured_launches;
+        b->shape = shape;
+    }
+    GS_CUDA(cudaMemcpyAsync(b->uniforms_dev.ptr, b->uniforms_host, (size_t)n * sizeof(gs_frame_uniforms),
+                            cudaMemcpyHostToDevice, st));
+    GS_CUDA(cudaGraphLaunch(b->exec, st));
+    gs::g_launches.fetch_add(b->graph_launches, std::memory_order_relaxed);
+    b->last.assign(views, views + n);
+    return GS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+gs_status gs_batch_create(gs_multi_viewer *mv, const char *const *keys, uint32_t key_count, gs_batch **out) {
+    if (!mv || !out || (key_count && !keys)) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    gs_batch *b = new gs_batch();
+    b->mv = mv;
+    for (uint32_t i = 0; i < key_count; ++i) {
+        if (!keys[i]) {
+            delete b;
+            return fail(GS_ERR_INVALID_ARG, "key %u is NULL", i);
+        }
+        b->keys.emplace_back(keys[i]);
+    }
+    *out = b;
+    return GS_OK;
+}
+
+void gs_batch_destroy(gs_batch *b) {
+    if (!b) return;
+    cudaDeviceSynchronize();
+    delete b;
+}
+
+gs_status gs_batch_render(gs_batch *b, const gs_batch_view *views, uint32_t view_count, gs_stream stream) {
+    if (!b || (view_count && !views)) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(b->mu);
+    return batch_render_locked(b, views, view_count, (cudaStream_t)stream);
+}
+
+gs_status gs_batch_synchronize(gs_batch *b, gs_stream stream) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "batch is NULL");
+    std::lock_guard<std::mutex> g(b->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        GS_CUDA(cudaStreamSynchronize(st));
+        bool regrow = false;
+        for (size_t i = 0; i < b->last.size(); ++i) {
+            ViewSlot &v = b->slots[i];
+            Ctrl c{}, a{}, s{};
+            GS_CUDA(cudaMemcpy(&c, v.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+            GS_CUDA(cudaMemcpy(&a, v.pre_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+            GS_CUDA(cudaMemcpy(&s, v.sort_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+            const uint32_t bits = c.status | a.status | s.status;
+            if (bits & kStatusTimeout) return status_from_bits(bits, "batch");
+            if (bits & kStatusCapacity) {
+                uint64_t p = (uint64_t)c.total + c.total / 4 + 4096;
+                v.max_pairs = p > 0x7FFFFFFFull ? 0x7FFFFFFFu : (uint32_t)p;
+                v.raster_scratch.release();
+                regrow = true;
+            }
+        }
+        if (!regrow) return GS_OK;
+        std::vector<gs_batch_view> again = b->last;
+        const gs_status s = batch_render_locked(b, again.data(), (uint32_t)again.size(), st);
+        if (s != GS_OK) return s;
+    }
+    return fail(GS_ERR_CAPACITY, "tile-pair list kept overflowing");
+}
+
+}  // extern "C"
+
+// ---- Serving: resident scenes, admission by per-view memory, overlapping requests ------------
+namespace {
+
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Device bytes one request holds while admitted: its key/index/splat buffers, scratch of the
+// three stages (tile-pair list at the default capacity) and its render target.
+size_t request_bytes(uint32_t n, uint32_t w, uint32_t h) {
+    return (size_t)n * (4 + 4 + sizeof(gs_splat)) + preprocess_scratch_bytes(n) + sort_scratch_bytes(n, 32) +
+           raster_scratch_bytes(n, w, h, default_pairs(n, w, h)) + (size_t)w * h * 4;
+}
+
+struct ServerReq {
+    const Model *model = nullptr;
+    gs_camera_pod camera{};
+    uint32_t w = 0, h = 0, pitch = 0;
+    uint8_t *out = nullptr;
+    int out_on_host = 0;
+    size_t bytes = 0;
+    double t_submit = 0, t_done = 0;
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+    int slot = -1;
+};
+
+struct ServerSlot {
+    ViewSlot view;
+    DevBuf target;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    uint64_t req = 0;
+    bool busy = false;
+};
+
+}  // namespace
+
+struct gs_server {
+    gs_multi_viewer *mv = nullptr;
+    size_t budget = 0, reserved = 0;
+    std::vector<ServerSlot> slots;
+    std::deque<uint64_t> queue;
+    std::unordered_map<uint64_t, ServerReq> reqs;
+    std::vector<double> lat;
+    uint64_t next = 1, completed = 0, failed = 0;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv, done_cv;
+    bool stop = false;
+    gs_status error = GS_OK;
+
+    ~gs_server() {
+        {
+            std::lock_guard<std::mutex> g(mu);
+            stop = true;
+        }
+        cv.notify_all();
+        if (worker.joinable()) worker.join();
+        for (auto &sl : slots) {
+            if (sl.stream) {
+                cudaStreamSynchronize(sl.stream);
+                cudaStreamDestroy(sl.stream);
+            }
+            if (sl.done) cudaEventDestroy(sl.done);
+        }
+    }
+};
+
+namespace {
+
+// Enqueue one admitted request on its slot's stream (scheduler thread, server lock held).
+gs_status server_launch(gs_server *sv, ServerReq &r, ServerSlot &sl) {
+    bool changed = false;
+    GS_CUDA(sl.view.prepare(r.model, r.w, r.h, &changed));
+    uint8_t *target = r.out;
+    uint32_t pitch = r.pitch;
+    if (r.out_on_host || !r.out) {
+        GS_CUDA(sl.target.ensure((size_t)r.w * r.h * 4));
+        target = (uint8_t *)sl.target.ptr;
+        pitch = r.w * 4;
+    }
+    gs_gaussian_transform_pod gt;
+    {
+        std::lock_guard<std::mutex> g(sv->mv->mu);
+        gt = sv->mv->frame.gt;
+    }
+    gs_frame_uniforms u;
+    gs_status s = gs_frame_uniforms_build(&r.camera, &r.model->model, &gt, r.w, r.h, &u);
+    if (s != GS_OK) return s;
+    const Model *m = r.model;
+    ViewSlot &v = sl.view;
+    uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+    cudaError_t e = launch_preprocess(u, m->records.ptr, m->format, m->n,
+                                      m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert, ind,
+                                      ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr, gs_depth_capacity(m->n),
+                                      (gs_splat *)v.splats.ptr, v.pre_scratch.ptr, sl.stream);
+    if (e == cudaSuccess)
+        e = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, 32, v.sort_scratch.ptr,
+                        sl.stream);
+    if (e == cudaSuccess) {
+        const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
+        e = launch_raster(&seg, 1, u, target, r.w, r.h, pitch, v.max_pairs, v.raster_scratch.ptr,
+                          sv->mv->frame.exact_exp, sl.stream);
+    }
+    if (e == cudaSuccess && r.out_on_host && r.out)
+        e = cudaMemcpyAsync(r.out, target, (size_t)r.w * r.h * 4, cudaMemcpyDeviceToHost, sl.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(sl.done, sl.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "server launch");
+    return GS_OK;
+}
+
+void server_loop(gs_server *sv) {
+    std::unique_lock<std::mutex> lk(sv->mu);
+    while (!sv->stop) {
+        bool busy = false;
+        // completions
+        for (size_t i = 0; i < sv->slots.size(); ++i) {
+            ServerSlot &sl = sv->slots[i];
+            if (!sl.busy) continue;
+            const cudaError_t q = cudaEventQuery(sl.done);
+            if (q == cudaErrorNotReady) {
+                busy = true;
+                continue;
+            }
+            ServerReq &r = sv->reqs[sl.req];
+            r.t_done = now_ms();
+            Ctrl c{};
+            uint32_t bits = 0;
+            if (q == cudaSuccess && cudaMemcpy(&c, sl.view.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost) == cudaSuccess)
+                bits = c.status;
+            if (q != cudaSuccess || (bits & kStatusTimeout)) {
+                r.state = 3;
+                ++sv->failed;
+            } else if (bits & kStatusCapacity) {
+                // grow this slot's tile-pair list and run the request again
+                uint64_t p = (uint64_t)c.total + c.total / 4 + 4096;
+                sl.view.max_pairs = p > 0x7FFFFFFFull ? 0x7FFFFFFFu : (uint32_t)p;
+                sl.view.raster_scratch.release();
+                if (server_launch(sv, r, sl) == GS_OK) {
+                    busy = true;
+                    continue;
+                }
+                r.state = 3;
+                ++sv->failed;
+            } else {
+                r.state = 2;
+                ++sv->completed;
+                sv->lat.push_back(r.t_done - r.t_submit);
+            }
+            sv->reserved -= r.bytes;
+            sl.busy = false;
+            sv->done_cv.notify_all();
+        }
+        // admissions, first come first served, while memory and a slot are free
+        while (!sv->queue.empty()) {
+            ServerReq &r = sv->reqs[sv->queue.front()];
+            if (sv->reserved > 0 && sv->reserved + r.bytes > sv->budget) break;
+            int free_slot = -1;
+            for (size_t i = 0; i < sv->slots.size(); ++i)
+                if (!sv->slots[i].busy) {
+                    free_slot = (int)i;
+                    break;
+                }
+            if (free_slot < 0) break;
+            ServerSlot &sl = sv->slots[free_slot];
+            const uint64_t id = sv->queue.front();
+            sv->queue.pop_front();
+            r.slot = free_slot;
+            r.state = 1;
+            sv->reserved += r.bytes;
+            sl.busy = true;
+            sl.req = id;
+            if (server_launch(sv, r, sl) != GS_OK) {
+                r.state = 3;
+                ++sv->failed;
+                sv->reserved -= r.bytes;
+                sl.busy = false;
+                sv->done_cv.notify_all();
+            } else {
+                busy = true;
+            }
+        }
+        if (busy) {
+            lk.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            lk.lock();
+        } else {
+            sv->cv.wait_for(lk, std::chrono::milliseconds(5));
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+gs_status gs_server_create(gs_multi_viewer *mv, size_t budget_bytes, uint32_t max_inflight, gs_server **out) {
+    if (!mv || !out || max_inflight == 0) return fail(GS_ERR_INVALID_ARG, "invalid server arguments");
+    gs_server *sv = new gs_server();
+    sv->mv = mv;
+    sv->budget = budget_bytes;
+    sv->slots.resize(max_inflight);
+    for (auto &sl : sv->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            delete sv;
+            return cuda_fail(e, "server streams");
+        }
+    }
+    sv->worker = std::thread(server_loop, sv);
+    *out = sv;
+    return GS_OK;
+}
+
+void gs_server_destroy(gs_server *sv) { delete sv; }
+
+gs_status gs_server_submit(gs_server *sv, const char *key, const gs_camera_pod *camera, uint32_t width, uint32_t height,
+                           uint8_t *out, uint32_t out_pitch, int out_on_host, uint64_t *ticket) {
+    if (!sv || !key || !camera || !ticket || width == 0 || height == 0) return fail(GS_ERR_INVALID_ARG, "invalid request");
+    if (out && !out_on_host && (out_pitch < 4 * width || out_pitch % 4 || !aligned(out, 4)))
+        return fail(GS_ERR_INVALID_ARG, "invalid output pitch");
+    const Model *m = nullptr;
+    {
+        std::lock_guard<std::mutex> g(sv->mv->mu);
+        auto it = sv->mv->models.find(key);
+        if (it == sv->mv->models.end()) return fail(GS_ERR_NOT_FOUND, "model '%s' not found", key);
+        m = it->second;
+    }
+    ServerReq r;
+    r.model = m;
+    r.camera = *camera;
+    r.w = width;
+    r.h = height;
+    r.out = out;
+    r.pitch = out_pitch;
+    r.out_on_host = out_on_host;
+    r.bytes = request_bytes(m->n, width, height);
+    if (r.bytes > sv->budget) return fail(GS_ERR_ADMISSION, "request needs %zu bytes, budget is %zu", r.bytes, sv->budget);
+    r.t_submit = now_ms();
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        const uint64_t id = sv->next++;
+        sv->reqs.emplace(id, r);
+        sv->queue.push_back(id);
+        *ticket = id;
+    }
+    sv->cv.notify_all();
+    return GS_OK;
+}
+
+gs_status gs_server_wait(gs_server *sv, uint64_t ticket, double timeout_s, double *latency_ms) {
+    if (!sv) return fail(GS_ERR_INVALID_ARG, "server is NULL");
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->reqs.find(ticket);
+    if (it == sv->reqs.end()) return fail(GS_ERR_NOT_FOUND, "unknown ticket");
+    const bool ok = sv->done_cv.wait_for(lk, std::chrono::duration<double>(timeout_s),
+                                         [&] { return it->second.state >= 2; });
+    if (!ok) return fail(GS_ERR_TIMEOUT, "request still running after %.3f s", timeout_s);
+    if (latency_ms) *latency_ms = it->second.t_done - it->second.t_submit;
+    const int state = it->second.state;
+    sv->reqs.erase(it);
+    return state == 2 ? GS_OK : fail(GS_ERR_CUDA, "request failed on the device");
+}
+
+gs_status gs_server_stats(gs_server *sv, gs_server_report *out) {
+    if (!sv || !out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(sv->mu);
+    out->completed = sv->completed;
+    out->failed = sv->failed;
+    out->queued = (uint32_t)sv->queue.size();
+    uint32_t running = 0;
+    for (auto &sl : sv->slots) running += sl.busy ? 1u : 0u;
+    out->running = running;
+    out->reserved_bytes = sv->reserved;
+    std::vector<double> l = sv->lat;
+    std::sort(l.begin(), l.end());
+    auto pct = [&](double q) { return l.empty() ? 0.0 : l[std::min(l.size() - 1, (size_t)(q * (l.size() - 1) + 0.5))]; };
+    out->p50_ms = pct(0.50);
+    out->p99_ms = pct(0.99);
+    double sum = 0;
+    for (double x : l) sum += x;
+    out->mean_ms = l.empty() ? 0.0 : sum / l.size();
+    out->max_ms = l.empty() ? 0.0 : l.back();
+    return GS_OK;
+}
+
+gs_status gs_server_reset_stats(gs_server *sv) {
+    if (!sv) return fail(GS_ERR_INVALID_ARG, "server is NULL");
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->lat.clear();
+    sv->completed = 0;
+    sv->failed = 0;
+    return GS_OK;
+}
+
+size_t gs_server_request_bytes(uint32_t n, uint32_t width, uint32_t height) { return request_bytes(n, width, height); }
 
 }  // extern "C"

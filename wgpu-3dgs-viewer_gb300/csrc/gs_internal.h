@@ -34,7 +34,8 @@ size_t preprocess_scratch_bytes(uint32_t n);
 cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, uint32_t format,
                               uint32_t n, const uint32_t *selection, int invert, uint32_t *indirect,
                               uint32_t *dispatch, uint32_t *indices, float *depths,
-                              uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st);
+                              uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st,
+                              const gs_frame_uniforms *u_dev = nullptr);
 
 // ---- K2 onesweep radix sort (gs_sort.cu) ----
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits);

@@ -19,6 +19,7 @@ constexpr uint32_t kPreThreads = 128;
 
 struct PreParams {
     gs_frame_uniforms u;
+    const gs_frame_uniforms *u_dev;  // when set (graph-captured batches), uniforms are read here
     const uint8_t *records;
     uint32_t n;
     uint32_t ntiles;
@@ -305,14 +306,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
-template <uint32_t FMT>
+template <uint32_t FMT, bool DEV_UNIFORMS>
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_constant__ PreParams P) {
     constexpr uint32_t REC = (FMT == GS_FORMAT_FP32) ? 224u : 128u;
     __shared__ __align__(128) uint8_t s_rec[kPreThreads * REC];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_tile, s_epoch, s_base, s_warp[kPreThreads / 32];
+    __shared__ __align__(16) gs_frame_uniforms s_u;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const gs_frame_uniforms &u = P.u;
+    if constexpr (DEV_UNIFORMS) {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(P.u_dev);
+        for (uint32_t i = tid; i < sizeof(gs_frame_uniforms) / 4; i += kPreThreads)
+            reinterpret_cast<uint32_t *>(&s_u)[i] = src[i];
+    }
+    const gs_frame_uniforms &u = DEV_UNIFORMS ? s_u : P.u;
 
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&P.ctrl->epoch;
@@ -504,7 +511,8 @@ size_t preprocess_scratch_bytes(uint32_t n) {
 cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, uint32_t format,
                               uint32_t n, const uint32_t *selection, int invert, uint32_t *indirect,
                               uint32_t *dispatch, uint32_t *indices, float *depths,
-                              uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st) {
+                              uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st,
+                              const gs_frame_uniforms *u_dev) {
     Ctrl *ctrl = reinterpret_cast<Ctrl *>(scratch);
     uint64_t *flags = reinterpret_cast<uint64_t *>((uint8_t *)scratch + align_up(sizeof(Ctrl), 256));
     ctrl_init_kernel<<<1, 256, 0, st>>>(ctrl, 1);
@@ -516,6 +524,7 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
     }
     PreParams P;
     P.u = u;
+    P.u_dev = u_dev;
     P.records = reinterpret_cast<const uint8_t *>(records);
     P.n = n;
     P.ntiles = (n + kPreThreads - 1) / kPreThreads;
@@ -531,16 +540,30 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
     P.flags = flags;
     prof_mark(kProfPreprocess, true, st);
     count_launches(1);
-    switch (format) {
-        case GS_FORMAT_FP32:
-            preprocess_kernel<GS_FORMAT_FP32><<<P.ntiles, kPreThreads, 0, st>>>(P);
-            break;
-        case GS_FORMAT_HALF_SH_FP16:
-            preprocess_kernel<GS_FORMAT_HALF_SH_FP16><<<P.ntiles, kPreThreads, 0, st>>>(P);
-            break;
-        default:
-            preprocess_kernel<GS_FORMAT_HALF_SH_BF16><<<P.ntiles, kPreThreads, 0, st>>>(P);
-            break;
+    if (u_dev) {
+        switch (format) {
+            case GS_FORMAT_FP32:
+                preprocess_kernel<GS_FORMAT_FP32, true><<<P.ntiles, kPreThreads, 0, st>>>(P);
+                break;
+            case GS_FORMAT_HALF_SH_FP16:
+                preprocess_kernel<GS_FORMAT_HALF_SH_FP16, true><<<P.ntiles, kPreThreads, 0, st>>>(P);
+                break;
+            default:
+                preprocess_kernel<GS_FORMAT_HALF_SH_BF16, true><<<P.ntiles, kPreThreads, 0, st>>>(P);
+                break;
+        }
+    } else {
+        switch (format) {
+            case GS_FORMAT_FP32:
+                preprocess_kernel<GS_FORMAT_FP32, false><<<P.ntiles, kPreThreads, 0, st>>>(P);
+                break;
+            case GS_FORMAT_HALF_SH_FP16:
+                preprocess_kernel<GS_FORMAT_HALF_SH_FP16, false><<<P.ntiles, kPreThreads, 0, st>>>(P);
+                break;
+            default:
+                preprocess_kernel<GS_FORMAT_HALF_SH_BF16, false><<<P.ntiles, kPreThreads, 0, st>>>(P);
+                break;
+        }
     }
     prof_mark(kProfPreprocess, false, st);
     return cudaGetLastError();

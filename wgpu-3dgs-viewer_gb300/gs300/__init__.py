@@ -36,7 +36,7 @@ from .records import (
 __all__ = [
     "Camera", "CameraPod", "GaussianTransformPod", "ModelTransformPod", "FrameUniforms", "Viewer",
     "MultiModelViewer", "RenderTarget", "Preprocessor", "RadixSorter", "Renderer", "GsError",
-    "ModelNotFound", "GaussianDisplayMode", "pack_gaussians", "frame_uniforms",
+    "ModelNotFound", "GaussianDisplayMode", "pack_gaussians", "frame_uniforms", "Batch", "Server",
 ]
 
 
@@ -327,6 +327,97 @@ class MultiModelViewer:
     def close(self):
         if getattr(self, "_h", None):
             lib().gs_multi_viewer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many views (model key, camera, target) of a MultiModelViewer rendered by one CUDA graph per
+    batch shape; no counterpart in the reference."""
+
+    def __init__(self, viewer, keys):
+        self.viewer = viewer  # keeps the models alive
+        self.keys = list(keys)
+        arr = (ctypes.c_char_p * max(1, len(self.keys)))(*[k.encode() for k in self.keys])
+        h = ctypes.c_void_p()
+        check(lib().gs_batch_create(viewer._h, arr, len(self.keys), ctypes.byref(h)))
+        self._h = h
+
+    def render(self, views, stream=None):
+        """views: iterable of (key or model index, CameraPod, target)."""
+        views = list(views)
+        arr = (records.BatchView * max(1, len(views)))()
+        for i, (model, pod, target) in enumerate(views):
+            idx = self.keys.index(model) if isinstance(model, str) else int(model)
+            ptr, w, h, pitch = _target_args(target)
+            arr[i].model, arr[i].width, arr[i].height, arr[i].pitch = idx, w, h, pitch
+            arr[i].target = ptr
+            arr[i].camera = pod
+        check(lib().gs_batch_render(self._h, ctypes.cast(arr, ctypes.c_void_p), len(views), _stream(stream)))
+
+    def synchronize(self, stream=None):
+        check(lib().gs_batch_synchronize(self._h, _stream(stream)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Request loop over resident scenes (the models of a MultiModelViewer): requests are admitted
+    while their per-view memory fits `budget_bytes` and a slot is free, and overlap on the device."""
+
+    def __init__(self, viewer, budget_bytes, max_inflight=8):
+        self.viewer = viewer
+        h = ctypes.c_void_p()
+        check(lib().gs_server_create(viewer._h, int(budget_bytes), int(max_inflight), ctypes.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def request_bytes(n, width, height):
+        return lib().gs_server_request_bytes(int(n), int(width), int(height))
+
+    def submit(self, key, camera_pod, width, height, out=None):
+        """Queue a request; `out` may be a host numpy (H, W, 4) uint8 array or a torch CUDA tensor."""
+        ticket = ctypes.c_uint64()
+        if out is None:
+            ptr, pitch, host = None, 0, 0
+        elif isinstance(out, np.ndarray):
+            ptr, pitch, host = out.ctypes.data_as(ctypes.c_void_p), 0, 1
+        else:
+            ptr, pitch, host = ctypes.c_void_p(int(out.data_ptr())), int(out.stride(0)), 0
+        check(lib().gs_server_submit(self._h, key.encode(), ref(camera_pod), int(width), int(height), ptr, pitch, host,
+                                     ctypes.byref(ticket)))
+        return ticket.value
+
+    def wait(self, ticket, timeout_s=60.0):
+        lat = ctypes.c_double()
+        check(lib().gs_server_wait(self._h, ctypes.c_uint64(ticket), float(timeout_s), ctypes.byref(lat)))
+        return lat.value
+
+    def stats(self):
+        r = records.ServerReport()
+        check(lib().gs_server_stats(self._h, ref(r)))
+        return {f: getattr(r, f) for f, _ in records.ServerReport._fields_}
+
+    def reset_stats(self):
+        check(lib().gs_server_reset_stats(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gs_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -94,6 +94,17 @@ SIGNATURES = [
     ("gs_multi_viewer_update_gaussian_transform_with_pod", ST, [P, P]),
     ("gs_multi_viewer_render", ST, [P, ctypes.POINTER(CP), U32, P, U32, U32, U32, P]),
     ("gs_multi_viewer_synchronize", ST, [P, P]),
+    ("gs_batch_create", ST, [P, ctypes.POINTER(CP), U32, PP]),
+    ("gs_batch_destroy", None, [P]),
+    ("gs_batch_render", ST, [P, P, U32, P]),
+    ("gs_batch_synchronize", ST, [P, P]),
+    ("gs_server_create", ST, [P, SZ, U32, PP]),
+    ("gs_server_destroy", None, [P]),
+    ("gs_server_request_bytes", SZ, [U32, U32, U32]),
+    ("gs_server_submit", ST, [P, CP, P, U32, U32, P, U32, I32, ctypes.POINTER(ctypes.c_uint64)]),
+    ("gs_server_wait", ST, [P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    ("gs_server_stats", ST, [P, P]),
+    ("gs_server_reset_stats", ST, [P]),
 ]
 
 _lib = None

@@ -143,3 +143,32 @@ def sh_degree_checked(deg):
     if not (0 <= int(deg) <= 3):
         raise ValueError(f"SH degree {deg} out of range 0..=3")
     return int(deg)
+
+
+class BatchView(ctypes.Structure):
+    """gs_batch_view: one view of a batch (model index, RGBA8 target, camera)."""
+
+    _fields_ = [
+        ("model", ctypes.c_uint32),
+        ("width", ctypes.c_uint32),
+        ("height", ctypes.c_uint32),
+        ("pitch", ctypes.c_uint32),
+        ("target", ctypes.c_void_p),
+        ("camera", CameraPod),
+    ]
+
+
+class ServerReport(ctypes.Structure):
+    """gs_server_report: request counts and submit-to-completion latency percentiles."""
+
+    _fields_ = [
+        ("completed", ctypes.c_uint64),
+        ("failed", ctypes.c_uint64),
+        ("queued", ctypes.c_uint32),
+        ("running", ctypes.c_uint32),
+        ("reserved_bytes", ctypes.c_uint64),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+    ]
