@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=6)
     ap.add_argument("--cpu-baseline-frames", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tiers", action="store_true")
+    ap.add_argument("--batch-views", type=int, default=8)
+    ap.add_argument("--serve-inflight", type=int, default=4)
     return ap.parse_args()
 
 
@@ -156,6 +159,117 @@ def cpu_baseline(args, scene, pods, threads):
     }
 
 
+def measure_tiers(args, scene, pods, stream, plain_fps):
+    """The tiers built on the plain path, on the same workload: multi-view batches (one CUDA graph
+    per batch shape), compressed records (FP16 rotation/scale, BF16 SH), and serving (open-loop
+    Poisson arrivals at 80% of the measured peak request rate, p50/p99 latency)."""
+    import torch
+
+    import gs300
+    from gs300 import records as R
+    from gs300 import scene as S
+
+    W, H, B = args.width, args.height, args.batch_views
+    sh = stream.cuda_stream
+    out = {"plain_fp32_fps": plain_fps}
+
+    def batch_fps(mv, key, reps):
+        batch = gs300.Batch(mv, [key])
+        targets = [gs300.RenderTarget(W, H) for _ in range(B)]
+
+        def go(r):
+            batch.render([(key, pods[(r * B + i) % 120], targets[i]) for i in range(B)], stream=sh)
+
+        go(0)
+        batch.synchronize(stream=sh)
+        for r in range(2):
+            go(r)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for r in range(reps):
+            go(r)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        batch.synchronize(stream=sh)
+        fps = B * reps / (e0.elapsed_time(e1) / 1000.0)
+        batch.close()
+        return fps
+
+    def plain_fps_of(viewer, reps):
+        t = gs300.RenderTarget(W, H)
+        for k in range(3):
+            viewer.update_camera_with_pod(pods[k])
+            viewer.render(t, stream=sh)
+            viewer.synchronize(stream=sh)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(reps):
+            viewer.update_camera_with_pod(pods[k % 120])
+            viewer.render(t, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return reps / (e0.elapsed_time(e1) / 1000.0)
+
+    reps = max(2, args.steps // B)
+    mv32 = gs300.MultiModelViewer()
+    mv32.insert_model("scene", scene)
+    out["batched_fp32_fps"] = batch_fps(mv32, "scene", reps)
+    out["batch_views"] = B
+    mv32.close()
+
+    half = S.synth_scene(args.n, seed=args.seed, fmt=R.FORMAT_HALF_SH_BF16)
+    v16 = gs300.Viewer(half, fmt=R.FORMAT_HALF_SH_BF16)
+    out["plain_fp16_fps"] = plain_fps_of(v16, args.steps)
+    v16.close()
+    mv16 = gs300.MultiModelViewer()
+    mv16.insert_model("scene", half, fmt=R.FORMAT_HALF_SH_BF16)
+    out["batched_fp16_fps"] = batch_fps(mv16, "scene", reps)
+
+    # serving: closed loop to find the peak request rate, then Poisson arrivals at 80% of it
+    need = gs300.Server.request_bytes(args.n, W, H)
+    sv = gs300.Server(mv16, budget_bytes=need * args.serve_inflight, max_inflight=args.serve_inflight)
+    for k in range(args.serve_inflight):
+        sv.wait(sv.submit("scene", pods[k], W, H))
+    sv.reset_stats()
+    n_req = max(4 * args.serve_inflight, args.steps)
+    t0 = time.perf_counter()
+    tickets = [sv.submit("scene", pods[k % 120], W, H) for k in range(n_req)]
+    for t in tickets:
+        sv.wait(t)
+    peak = n_req / (time.perf_counter() - t0)
+    sv.reset_stats()
+    rate = 0.8 * peak
+    rng = np.random.default_rng(1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_req))
+    tickets = []
+    t0 = time.perf_counter()
+    for k, at in enumerate(arrivals):
+        dt = at - (time.perf_counter() - t0)
+        if dt > 0:
+            time.sleep(dt)
+        tickets.append(sv.submit("scene", pods[k % 120], W, H))
+    for t in tickets:
+        sv.wait(t)
+    elapsed = time.perf_counter() - t0
+    st = sv.stats()
+    out["served_fp16"] = {
+        "peak_fps": peak,
+        "offered_rps": rate,
+        "fps": n_req / elapsed,
+        "p50_ms": st["p50_ms"],
+        "p99_ms": st["p99_ms"],
+        "max_ms": st["max_ms"],
+        "requests": n_req,
+        "max_inflight": args.serve_inflight,
+    }
+    sv.close()
+    mv16.close()
+    out["best_vs_plain_fp32"] = max(out["batched_fp32_fps"], out["batched_fp16_fps"], out["plain_fp16_fps"],
+                                    out["served_fp16"]["fps"]) / plain_fps
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -259,13 +373,17 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     l0 = gs300.launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
     for k in range(args.steps):
         frame(k)
-    e1.record(stream)
+        ev[k + 1].record(stream)
     torch.cuda.synchronize()
+    e0, e1 = ev[0], ev[-1]
     launches = gs300.launch_count() - l0
+    per_frame = sorted(ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps))
+    latency = {"p50": per_frame[len(per_frame) // 2], "p99": per_frame[min(len(per_frame) - 1, int(0.99 * len(per_frame)))],
+               "max": per_frame[-1], "what": "device time per plain frame (back to back)"}
     clock_info = clocks.stop()
     viewer.synchronize(stream=sh)
     ms = e0.elapsed_time(e1)
@@ -367,6 +485,10 @@ def main():
     e2e = {"value": world * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": 144,
            "d2h_bytes_per_step": W * H * 4}
 
+    tier_info = None
+    if not args.no_tiers and world == 1:
+        tier_info = measure_tiers(args, scene, pods, stream, value)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, scene, pods, os.cpu_count() or 1)
@@ -392,6 +514,8 @@ def main():
             "roofline": roofline,
             "stages": stages,
             "e2e": e2e,
+            "latency_ms": latency,
+            "tiers": tier_info,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
