@@ -38,7 +38,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gs300", choices=["gs300", "reference"])
-    ap.add_argument("--n", type=int, default=6_000_000)
+    ap.add_argument("--splats", "--n", dest="n", type=int, default=6_000_000)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--seed", type=int, default=6)
@@ -50,11 +50,10 @@ def parse():
     return ap.parse_args()
 
 
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+def replicas(backend):
+    from gs300.replicas import Replicas
+
+    return Replicas(backend)
 
 
 def workload(args):
@@ -271,9 +270,8 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
 
 
 def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
+    if not replicas(None).leader:
+        return  # the CPU arm runs on rank 0 alone; the other ranks exit without work
     from gs300 import records as R
     from gs300 import scene as S
     from oracle import oracle as O
@@ -341,14 +339,12 @@ def main():
     import gs300
     from gs300 import scene as S
 
-    rank, world, local = dist_env()
+    group = replicas("nccl")
+    rank, world, local = group.rank, group.world, group.local
     torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    group.init()
     W, H = args.width, args.height
-    scene = S.synth_scene(args.n, seed=args.seed + rank)
+    scene = S.synth_scene(args.n, seed=group.scene_seed(args.seed))
     viewer = gs300.Viewer(scene)
     target = gs300.RenderTarget(W, H)
     stream = torch.cuda.Stream()
@@ -359,9 +355,7 @@ def main():
         viewer.update_camera_with_pod(pods[k % 120])
         viewer.render(target, stream=sh)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    barrier = group.barrier
 
     for k in range(max(3, args.warmup)):
         frame(k)
@@ -388,12 +382,8 @@ def main():
     viewer.synchronize(stream=sh)
     ms = e0.elapsed_time(e1)
     barrier()
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1000.0)
+    value, s_max = group.job_rate(args.steps, ms / 1000.0)
+    ms_max = 1000.0 * s_max
 
     # ---- per-stage times (CUDA events around each stage on the launching stream) ----
     gs300.profile_enable(True)
@@ -477,12 +467,8 @@ def main():
         viewer.update_camera_with_pod(pods[k % 120])  # 144-byte CameraPod from host memory
         viewer.render(target, stream=sh)
         target.download(host, stream=sh)  # device -> pinned host, synchronises
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": 144,
+    e2e_rate, _ = group.job_rate(args.steps, time.perf_counter() - t0)
+    e2e = {"value": e2e_rate, "unit": "frames/s", "h2d_bytes_per_step": 144,
            "d2h_bytes_per_step": W * H * 4}
 
     tier_info = None
@@ -519,8 +505,7 @@ def main():
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    group.close()
 
 
 if __name__ == "__main__":
