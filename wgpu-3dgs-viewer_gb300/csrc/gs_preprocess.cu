@@ -6,11 +6,14 @@
 // once per Gaussian instead of six times per splat.  Compiled with -fmad=false: every FP32
 // multiply and add rounds on its own, in the order of the CPU oracle (oracle/gs_oracle.cpp).
 //
-// Layout: a CTA owns 128 consecutive Gaussians.  One thread stages the CTA's records
-// (128 x 224 B = 28 KiB, or 128 x 128 B for the compressed record) into shared memory with a
-// single cp.async.bulk copy completing on an mbarrier, then each thread works on its record
-// from shared memory.  Visible Gaussians are compacted in ascending index order with a warp
-// ballot, a block scan and a decoupled look-back across CTAs (virtual CTA ids from a ticket).
+// Layout: a CTA owns 128 consecutive Gaussians and stages their records in shared memory, one
+// record per row: FP32 records (224 B) with a single cp.async.bulk copy completing on an
+// mbarrier; half records (128 B) with coalesced 16-byte cp.async copies into rows padded to
+// 144 B.  Every thread reads its own row with 128-bit shared loads, so the 8 rows a quarter-warp
+// touches meet at most 2 to a bank (224-byte rows) or not at all (144-byte rows); dense
+// 128-byte rows would put a whole quarter-warp on one bank.  Visible Gaussians are compacted in ascending index
+// order with a warp ballot, a block scan and a decoupled look-back across CTAs (virtual CTA
+// ids from a ticket).
 #include "gs_internal.h"
 
 namespace gs {
@@ -64,23 +67,48 @@ __device__ __forceinline__ bool cull(float x, float y, float z) {
     return !(x >= -1.0f && y >= -1.0f && z >= 0.0f && x <= 1.0f && y <= 1.0f && z <= 1.0f);
 }
 
-// Unpacked record (FP32 values regardless of the stored format).
+// Record staged in a padded shared-memory row (16-byte chunks), with the fields every visible
+// Gaussian needs unpacked to FP32.  SH coefficients stay in the row until the colour pass.
 struct Rec {
     float pos[3];
     uint32_t color;
-    const float *sh32;      // FP32 record: SH in shared memory
-    const uint16_t *sh16;   // compressed record: SH bits in shared memory
+    const uint4 *row;
     float cov3d[6];
 };
 
 template <uint32_t FMT>
-__device__ __forceinline__ float sh_at(const Rec &g, int k) {
+__device__ __forceinline__ float sh_decode(uint32_t bits) {
     if constexpr (FMT == GS_FORMAT_FP32) {
-        return g.sh32[k];
+        return __uint_as_float(bits);
     } else if constexpr (FMT == GS_FORMAT_HALF_SH_FP16) {
-        return __half2float(__ushort_as_half(g.sh16[k]));
+        return __half2float(__ushort_as_half((unsigned short)bits));
     } else {
-        return __uint_as_float((uint32_t)g.sh16[k] << 16);
+        return __uint_as_float(bits << 16);
+    }
+}
+
+// SH coefficients [K0, K1) of the row into out[0 .. K1-K0), read as the few 16-byte chunks
+// that hold them.  Coefficient k sits at byte 16 + 4k (FP32 record) or 30 + 2k (half record).
+template <uint32_t FMT, int K0, int K1>
+__device__ __forceinline__ void sh_load(const uint4 *row, float *out) {
+    constexpr int B = (FMT == GS_FORMAT_FP32) ? 4 : 2;
+    constexpr int OFF = (FMT == GS_FORMAT_FP32) ? 16 : 30;
+    constexpr int C0 = (OFF + K0 * B) / 16, C1 = (OFF + K1 * B - 1) / 16;
+    uint32_t w[(C1 - C0 + 1) * 4];
+#pragma unroll
+    for (int c = C0; c <= C1; ++c) {
+        const uint4 v = row[c];
+        w[(c - C0) * 4 + 0] = v.x;
+        w[(c - C0) * 4 + 1] = v.y;
+        w[(c - C0) * 4 + 2] = v.z;
+        w[(c - C0) * 4 + 3] = v.w;
+    }
+#pragma unroll
+    for (int k = K0; k < K1; ++k) {
+        const int byte = OFF + k * B - C0 * 16;
+        uint32_t bits = w[byte >> 2];
+        if (B == 2) bits = (byte & 2) ? (bits >> 16) : (bits & 0xFFFFu);
+        out[k - K0] = sh_decode<FMT>(bits);
     }
 }
 
@@ -102,31 +130,34 @@ __device__ __forceinline__ void quat_to_mat3(const float *q, float *m) {
 }
 
 template <uint32_t FMT>
-__device__ __forceinline__ Rec load_rec(const uint8_t *s) {
+__device__ __forceinline__ Rec load_rec(const uint4 *row) {
     Rec g;
+    const uint4 head = row[0];
+    g.pos[0] = __uint_as_float(head.x);
+    g.pos[1] = __uint_as_float(head.y);
+    g.pos[2] = __uint_as_float(head.z);
+    g.color = head.w;
+    g.row = row;
     if constexpr (FMT == GS_FORMAT_FP32) {
-        const gs_gaussian_pod *p = reinterpret_cast<const gs_gaussian_pod *>(s);
-        g.pos[0] = p->pos[0];
-        g.pos[1] = p->pos[1];
-        g.pos[2] = p->pos[2];
-        g.color = p->color;
-        g.sh32 = p->sh;
-        g.sh16 = nullptr;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) g.cov3d[k] = p->cov3d[k];
+        // cov3d occupies bytes 196..219: chunk 12 (.y .z .w) and chunk 13 (.x .y .z)
+        const uint4 c12 = row[12], c13 = row[13];
+        g.cov3d[0] = __uint_as_float(c12.y);
+        g.cov3d[1] = __uint_as_float(c12.z);
+        g.cov3d[2] = __uint_as_float(c12.w);
+        g.cov3d[3] = __uint_as_float(c13.x);
+        g.cov3d[4] = __uint_as_float(c13.y);
+        g.cov3d[5] = __uint_as_float(c13.z);
     } else {
-        const gs_gaussian_pod_half *p = reinterpret_cast<const gs_gaussian_pod_half *>(s);
-        g.pos[0] = p->pos[0];
-        g.pos[1] = p->pos[1];
-        g.pos[2] = p->pos[2];
-        g.color = p->color;
-        g.sh32 = nullptr;
-        g.sh16 = p->sh;
+        // rot[4] at bytes 16..23, scale[3] at bytes 24..29 (chunk 1)
+        const uint4 c1 = row[1];
+        const uint16_t rot[4] = {(uint16_t)(c1.x & 0xFFFFu), (uint16_t)(c1.x >> 16), (uint16_t)(c1.y & 0xFFFFu),
+                                 (uint16_t)(c1.y >> 16)};
+        const uint16_t scale[3] = {(uint16_t)(c1.z & 0xFFFFu), (uint16_t)(c1.z >> 16), (uint16_t)(c1.w & 0xFFFFu)};
         float q[4], sc[3];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) q[k] = __half2float(__ushort_as_half(p->rot[k]));
+        for (int k = 0; k < 4; ++k) q[k] = __half2float(__ushort_as_half(rot[k]));
 #pragma unroll
-        for (int k = 0; k < 3; ++k) sc[k] = __half2float(__ushort_as_half(p->scale[k]));
+        for (int k = 0; k < 3; ++k) sc[k] = __half2float(__ushort_as_half(scale[k]));
         const float nrm = sqrtf(((q[0] * q[0] + q[1] * q[1]) + q[2] * q[2]) + q[3] * q[3]);
 #pragma unroll
         for (int k = 0; k < 4; ++k) q[k] = q[k] / nrm;
@@ -222,13 +253,17 @@ __device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec
     for (int ch = 0; ch < 3; ++ch)
         res[ch] = u.no_sh0 ? 0.5f : (float)((g.color >> (8 * ch)) & 0xFFu) / 255.0f;
     if (u.sh_deg >= 1) {
+        float s1[9];
+        sh_load<FMT, 0, 9>(g.row, s1);
 #pragma unroll
         for (int ch = 0; ch < 3; ++ch) {
-            float v = (-sh_at<FMT>(g, 0 * 3 + ch)) * y + sh_at<FMT>(g, 1 * 3 + ch) * z;
-            v = v - sh_at<FMT>(g, 2 * 3 + ch) * x;
+            float v = (-s1[0 * 3 + ch]) * y + s1[1 * 3 + ch] * z;
+            v = v - s1[2 * 3 + ch] * x;
             res[ch] = res[ch] + c1 * v;
         }
         if (u.sh_deg >= 2) {
+            float s2[15];
+            sh_load<FMT, 9, 24>(g.row, s2);
             const float xx = x * x, yy = y * y, zz = z * z;
             const float xy = x * y, yz = y * z, xz = x * z;
             const float k0 = 1.0925484f * xy, k1 = -1.0925484f * yz;
@@ -236,13 +271,15 @@ __device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec
             const float k3 = -1.0925484f * xz, k4 = 0.5462742f * (xx - yy);
 #pragma unroll
             for (int ch = 0; ch < 3; ++ch) {
-                float v = k0 * sh_at<FMT>(g, 3 * 3 + ch) + k1 * sh_at<FMT>(g, 4 * 3 + ch);
-                v = v + k2 * sh_at<FMT>(g, 5 * 3 + ch);
-                v = v + k3 * sh_at<FMT>(g, 6 * 3 + ch);
-                v = v + k4 * sh_at<FMT>(g, 7 * 3 + ch);
+                float v = k0 * s2[0 * 3 + ch] + k1 * s2[1 * 3 + ch];
+                v = v + k2 * s2[2 * 3 + ch];
+                v = v + k3 * s2[3 * 3 + ch];
+                v = v + k4 * s2[4 * 3 + ch];
                 res[ch] = res[ch] + v;
             }
             if (u.sh_deg >= 3) {
+                float s3[21];
+                sh_load<FMT, 24, 45>(g.row, s3);
                 const float m0 = (-0.5900436f * y) * (3.0f * xx - yy);
                 const float m1 = (2.8906114f * xy) * z;
                 const float m2 = (-0.4570458f * y) * ((4.0f * zz - xx) - yy);
@@ -252,12 +289,12 @@ __device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec
                 const float m6 = (-0.5900436f * x) * (xx - 3.0f * yy);
 #pragma unroll
                 for (int ch = 0; ch < 3; ++ch) {
-                    float v = m0 * sh_at<FMT>(g, 8 * 3 + ch) + m1 * sh_at<FMT>(g, 9 * 3 + ch);
-                    v = v + m2 * sh_at<FMT>(g, 10 * 3 + ch);
-                    v = v + m3 * sh_at<FMT>(g, 11 * 3 + ch);
-                    v = v + m4 * sh_at<FMT>(g, 12 * 3 + ch);
-                    v = v + m5 * sh_at<FMT>(g, 13 * 3 + ch);
-                    v = v + m6 * sh_at<FMT>(g, 14 * 3 + ch);
+                    float v = m0 * s3[0 * 3 + ch] + m1 * s3[1 * 3 + ch];
+                    v = v + m2 * s3[2 * 3 + ch];
+                    v = v + m3 * s3[3 * 3 + ch];
+                    v = v + m4 * s3[4 * 3 + ch];
+                    v = v + m5 * s3[5 * 3 + ch];
+                    v = v + m6 * s3[6 * 3 + ch];
                     res[ch] = res[ch] + v;
                 }
             }
@@ -268,7 +305,14 @@ __device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec
     rgba[3] = (float)((g.color >> 24) & 0xFFu) / 255.0f;
 }
 
-// ---- mbarrier + bulk copy (global -> shared) ----------------------------------------------
+// ---- global -> shared staging: 16-byte cp.async chunks, or a bulk copy on an mbarrier -----
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(bar);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
@@ -309,7 +353,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
 template <uint32_t FMT, bool DEV_UNIFORMS>
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_constant__ PreParams P) {
     constexpr uint32_t REC = (FMT == GS_FORMAT_FP32) ? 224u : 128u;
-    __shared__ __align__(128) uint8_t s_rec[kPreThreads * REC];
+    constexpr uint32_t C16 = REC / 16;  // 16-byte chunks per record
+    // FP32 records: one bulk copy of the CTA's records into dense rows (a quarter-warp's 128-bit
+    // reads of 224-byte rows meet at most 2 to a bank).  Half records: 16-byte cp.async chunks
+    // into rows padded to 144 bytes (dense 128-byte rows would put a quarter-warp on one bank).
+    constexpr bool BULK = (FMT == GS_FORMAT_FP32);
+    constexpr uint32_t ROW16 = BULK ? C16 : C16 + 1;
+    __shared__ __align__(16) uint4 s_rec[kPreThreads * ROW16];
     __shared__ __align__(8) uint64_t s_bar;
     __shared__ uint32_t s_tile, s_epoch, s_base, s_warp[kPreThreads / 32];
     __shared__ __align__(16) gs_frame_uniforms s_u;
@@ -324,18 +374,34 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&P.ctrl->epoch;
         s_tile = atomicAdd(&P.ctrl->ticket[0], 1u);
-        mbar_init(&s_bar, 1);
+        if (BULK) mbar_init(&s_bar, 1);
     }
     __syncthreads();
     const uint32_t tile = s_tile, epoch = s_epoch;
     const uint32_t first = tile * kPreThreads;
     const uint32_t cnt = min(kPreThreads, P.n - first);
-    if (tid == 0) {
-        const uint32_t bytes = cnt * REC;
-        mbar_expect_tx(&s_bar, bytes);
-        bulk_g2s(s_rec, P.records + (size_t)first * REC, bytes, &s_bar);
+    if constexpr (BULK) {
+        if (tid == 0) {
+            mbar_expect_tx(&s_bar, cnt * REC);
+            bulk_g2s(s_rec, P.records + (size_t)first * REC, cnt * REC, &s_bar);
+        }
+        if (!mbar_wait(&s_bar, 0)) atomicOr(&P.ctrl->status, kStatusTimeout);
+    } else {
+        // consecutive threads copy consecutive 16-byte chunks (coalesced); chunk q of the CTA
+        // is chunk q % C16 of record q / C16
+        const uint4 *src = reinterpret_cast<const uint4 *>(P.records + (size_t)first * REC);
+        const uint32_t chunks = cnt * C16;
+#pragma unroll
+        for (uint32_t k = 0; k < C16; ++k) {
+            const uint32_t q = tid + k * kPreThreads;
+            if (q < chunks) {
+                const uint32_t r = q / C16;
+                cp_async16(&s_rec[r * ROW16 + (q - r * C16)], src + q);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
     }
-    if (!mbar_wait(&s_bar, 0)) atomicOr(&P.ctrl->status, kStatusTimeout);
 
     const uint32_t i = first + tid;
     bool vis = false;
@@ -350,7 +416,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
             selected = (P.invert != 0u) != bit;
         }
         if (selected) {
-            g = load_rec<FMT>(s_rec + (size_t)tid * REC);
+            g = load_rec<FMT>(s_rec + tid * ROW16);
             const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
             float clip[4];
             mat4_vec(u.model, p4, world);
