@@ -93,6 +93,28 @@ gs_status gs_model_transform_pod_new(const float pos[3], const float rot_xyzw[4]
  * (DefaultGaussianPod, src/lib.rs:43-44): cov3d = R·S·Sᵀ·Rᵀ from (rot, scale). */
 gs_status gs_gaussian_pack(const gs_gaussian *gaussians, size_t count, gs_gaussian_pod *out_pods);
 
+/* ---- PLY ingest (Gaussians::read_from_file(path, GaussiansSource::Ply), wgpu-3dgs-core 0.6.0,
+ * un-vendored; called at examples/simple.rs:157-160 before Viewer::new) ---------------------
+ * The file's header is scanned on the host; the vertex block is converted into device records
+ * on the GPU.  Conversion: rgb = clamp(0.5 + SH_C0·f_dc, 0, 1) and a = sigmoid(opacity), each
+ * rounded to 8 bits (round half to even); scale = exp(scale_i); rotation (x, y, z, w) =
+ * (rot_1, rot_2, rot_3, rot_0) normalised; these in double precision and rounded once to
+ * float.  SH bands beyond the file's degree are zero.  The FP32 record's cov3d is the one
+ * gs_gaussian_pack computes; half records round rotation, scale and SH to binary16 (SH to
+ * bfloat16 for GS_FORMAT_HALF_SH_BF16), nearest even. */
+
+/* Scan a PLY header (`len` bytes of the file, at least through "end_header\n") into `out`.
+ * GS_ERR_INVALID_ARG for anything but binary_little_endian, a list property in or before the
+ * vertex element, a missing or non-float required property, an f_rest count other than
+ * 0, 9, 24 or 45, or a vertex stride above 4096 bytes.  Host only. */
+gs_status gs_ply_parse_header(const void *bytes, size_t len, gs_ply_layout *out_layout);
+
+/* Convert layout->count vertices at `vertices` (device memory, 4-byte aligned, holding
+ * count·stride bytes: the file from data_offset on) into `records` (device memory, 16-byte
+ * aligned, count records of `format`), on `stream`.  Asynchronous. */
+gs_status gs_ply_convert(const void *vertices, const gs_ply_layout *layout, uint32_t format,
+                         void *records, cudaStream_t stream);
+
 /* Derive the per-frame kernel uniforms (view-projection, model matrices, camera position,
  * decoded GaussianTransform) from the three pods and the viewport size.  The stage entry
  * points below take this struct by pointer (host memory). */
@@ -200,6 +222,12 @@ typedef struct gs_viewer gs_viewer;
  * default is the SFU exp. */
 gs_status gs_viewer_create(const void *host_records, uint32_t count, uint32_t format,
                            gs_viewer **out_viewer);
+/* Viewer::new over the Gaussians of a PLY file held in host memory (`len` bytes): header
+ * scan, one host-to-device copy of the vertex block, device conversion into `format`
+ * records.  GS_ERR_INVALID_ARG if the file is shorter than its header says. */
+gs_status gs_viewer_create_from_ply(const void *ply_bytes, size_t len, uint32_t format,
+                                    gs_viewer **out_viewer);
+
 void gs_viewer_destroy(gs_viewer *viewer);
 uint32_t gs_viewer_len(const gs_viewer *viewer);
 
@@ -259,6 +287,9 @@ void gs_multi_viewer_destroy(gs_multi_viewer *viewer);
 /* insert_model (src/multi_model.rs:352-390): a key replaces an existing model of that key. */
 gs_status gs_multi_viewer_insert_model(gs_multi_viewer *viewer, const char *key,
                                        const void *host_records, uint32_t count, uint32_t format);
+/* insert_model over the Gaussians of a PLY file in host memory (as gs_viewer_create_from_ply). */
+gs_status gs_multi_viewer_insert_model_from_ply(gs_multi_viewer *viewer, const char *key,
+                                                const void *ply_bytes, size_t len, uint32_t format);
 /* remove_model (src/multi_model.rs:392-395): GS_ERR_NOT_FOUND if absent. */
 gs_status gs_multi_viewer_remove_model(gs_multi_viewer *viewer, const char *key);
 uint32_t gs_multi_viewer_model_count(const gs_multi_viewer *viewer);

@@ -66,6 +66,24 @@ typedef struct gs_gaussian_pod_half {
     uint16_t _pad[4];
 } gs_gaussian_pod_half;
 
+/* Where the fields of one vertex of a standard 3D Gaussian splatting PLY file lie: binary
+ * little-endian vertex element with float properties x, y, z, f_dc_0..2, opacity, scale_0..2,
+ * rot_0..3 (w, x, y, z), and optionally f_rest_0..(3K-1) stored channel-major (K = 3, 8 or 15
+ * coefficients per channel for SH degree 1, 2, 3).  Other properties are skipped.  Offsets are
+ * byte offsets within a vertex.  Written by gs_ply_parse_header. */
+typedef struct gs_ply_layout {
+    uint64_t data_offset; /* byte offset of the first vertex in the file */
+    uint32_t count;       /* vertices */
+    uint32_t stride;      /* bytes per vertex */
+    uint32_t sh_rest;     /* K: f_rest coefficients per channel (0, 3, 8 or 15) */
+    int32_t pos[3];
+    int32_t f_dc[3];
+    int32_t opacity;
+    int32_t scale[3];
+    int32_t rot[4];       /* rot_0..rot_3 */
+    int32_t f_rest[45];   /* f_rest_0..f_rest_(3K-1); -1 beyond */
+} gs_ply_layout;
+
 /* Camera (src/camera.rs:16-29). */
 typedef struct gs_camera {
     float pos[3];

@@ -40,6 +40,7 @@ def _declare(L):
     L.oracle_render.restype = U
     L.oracle64_render.argtypes = [P, P, P, P, U, U, P, U, U, I]
     L.oracle64_render.restype = U
+    L.oracle_ply_convert.argtypes = [P, P, U, P]
 
 
 def _p(a):
@@ -128,6 +129,17 @@ def render64(camera_pod, model_pod, gt_pod, records, fmt, w, h, threads=0):
     v = lib().oracle64_render(_p(camera_pod), _p(model_pod), _p(gt_pod), _p(records), fmt, len(records), _p(img), w, h,
                               threads or nproc())
     return img, v
+
+
+def ply_convert(vertex_block, layout, fmt):
+    """PLY vertex block (bytes from layout.data_offset on) -> records of `fmt` (numpy)."""
+    from gs300.records import record_dtype
+
+    v = np.frombuffer(bytes(vertex_block), dtype=np.uint8)
+    assert len(v) >= layout.count * layout.stride
+    out = np.zeros(layout.count, record_dtype(fmt))
+    lib().oracle_ply_convert(_p(np.ascontiguousarray(v)), _p(layout), fmt, _p(out))
+    return out
 
 
 def exp_portable(x):

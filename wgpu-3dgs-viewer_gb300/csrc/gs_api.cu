@@ -158,8 +158,36 @@ struct Model {
     uint32_t *indirect() { return reinterpret_cast<uint32_t *>(control.ptr); }  // [0..4) args, [4..7) dispatch
 
     gs_status create(const void *host, uint32_t count, uint32_t fmt) {
-        if (!valid_format(fmt)) return fail(GS_ERR_INVALID_ARG, "unknown record format %u", fmt);
         if (count > 0 && !host) return fail(GS_ERR_INVALID_ARG, "records pointer is NULL");
+        const gs_status s = alloc(count, fmt);
+        if (s != GS_OK) return s;
+        if (n) GS_CUDA(cudaMemcpy(records.ptr, host, (size_t)n * record_bytes(fmt), cudaMemcpyHostToDevice));
+        return GS_OK;
+    }
+
+    // Records converted on the device from the vertex block of a PLY file in host memory.
+    gs_status create_from_ply(const void *bytes, size_t len, uint32_t fmt) {
+        gs_ply_layout L;
+        gs_status s = gs_ply_parse_header(bytes, len, &L);
+        if (s != GS_OK) return s;
+        const uint64_t block = (uint64_t)L.count * L.stride;
+        if (L.data_offset > len || block > len - L.data_offset)
+            return fail(GS_ERR_INVALID_ARG, "PLY file holds %zu bytes, its header needs %llu", len,
+                        (unsigned long long)(L.data_offset + block));
+        s = alloc(L.count, fmt);
+        if (s != GS_OK) return s;
+        if (!n) return GS_OK;
+        DevBuf vertices;
+        GS_CUDA(vertices.ensure(block));
+        GS_CUDA(cudaMemcpy(vertices.ptr, static_cast<const uint8_t *>(bytes) + L.data_offset, block,
+                           cudaMemcpyHostToDevice));
+        GS_CUDA(launch_ply_convert(vertices.ptr, L, fmt, records.ptr, nullptr));
+        GS_CUDA(cudaStreamSynchronize(nullptr));
+        return GS_OK;
+    }
+
+    gs_status alloc(uint32_t count, uint32_t fmt) {
+        if (!valid_format(fmt)) return fail(GS_ERR_INVALID_ARG, "unknown record format %u", fmt);
         n = count;
         format = fmt;
         model = gs_model_transform_pod{};
@@ -167,7 +195,6 @@ struct Model {
         model.scale[0] = model.scale[1] = model.scale[2] = 1.0f;
         const size_t rb = record_bytes(fmt);
         GS_CUDA(records.ensure((size_t)n * rb));
-        if (n) GS_CUDA(cudaMemcpy(records.ptr, host, (size_t)n * rb, cudaMemcpyHostToDevice));
         GS_CUDA(control.ensure(64));
         GS_CUDA(cudaMemset(control.ptr, 0, 64));
         GS_CUDA(indices.ensure((size_t)n * 4));
@@ -441,21 +468,7 @@ gs_status gs_gaussian_pack(const gs_gaussian *g, size_t count, gs_gaussian_pod *
         o.color = (uint32_t)g[i].color[0] | ((uint32_t)g[i].color[1] << 8) | ((uint32_t)g[i].color[2] << 16) |
                   ((uint32_t)g[i].color[3] << 24);
         std::memcpy(o.sh, g[i].sh, sizeof(o.sh));
-        // Σ = (R·S)(R·S)ᵀ, accumulated in double and rounded once.
-        const double x = g[i].rot[0], y = g[i].rot[1], z = g[i].rot[2], w = g[i].rot[3];
-        const double R[3][3] = {{1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)},
-                                {2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)},
-                                {2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)}};
-        double M[3][3];
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) M[r][c] = R[r][c] * (double)g[i].scale[c];
-        auto cv = [&](int a, int b) { return (float)(M[a][0] * M[b][0] + M[a][1] * M[b][1] + M[a][2] * M[b][2]); };
-        o.cov3d[0] = cv(0, 0);
-        o.cov3d[1] = cv(0, 1);
-        o.cov3d[2] = cv(0, 2);
-        o.cov3d[3] = cv(1, 1);
-        o.cov3d[4] = cv(1, 2);
-        o.cov3d[5] = cv(2, 2);
+        cov3d_from_rot_scale(g[i].rot, g[i].scale, o.cov3d);
     }
     return GS_OK;
 }
@@ -619,6 +632,19 @@ gs_status gs_viewer_create(const void *host_records, uint32_t count, uint32_t fo
     if (!out) return fail(GS_ERR_INVALID_ARG, "out is NULL");
     gs_viewer *v = new gs_viewer();
     const gs_status s = v->model.create(host_records, count, format);
+    if (s != GS_OK) {
+        delete v;
+        return s;
+    }
+    v->frame.exact_exp = getenv("GS300_EXACT_EXP") ? 1 : 0;
+    *out = v;
+    return GS_OK;
+}
+
+gs_status gs_viewer_create_from_ply(const void *ply_bytes, size_t len, uint32_t format, gs_viewer **out) {
+    if (!out || !ply_bytes) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    gs_viewer *v = new gs_viewer();
+    const gs_status s = v->model.create_from_ply(ply_bytes, len, format);
     if (s != GS_OK) {
         delete v;
         return s;
@@ -841,15 +867,7 @@ void gs_multi_viewer_destroy(gs_multi_viewer *v) {
     delete v;
 }
 
-gs_status gs_multi_viewer_insert_model(gs_multi_viewer *v, const char *key, const void *host, uint32_t count,
-                                       uint32_t format) {
-    if (!v || !key) return fail(GS_ERR_INVALID_ARG, "NULL argument");
-    Model *m = new Model();
-    const gs_status s = m->create(host, count, format);
-    if (s != GS_OK) {
-        delete m;
-        return s;
-    }
+static gs_status multi_insert(gs_multi_viewer *v, const char *key, Model *m) {
     std::lock_guard<std::mutex> g(v->mu);
     auto it = v->models.find(key);
     if (it != v->models.end()) {
@@ -860,6 +878,30 @@ gs_status gs_multi_viewer_insert_model(gs_multi_viewer *v, const char *key, cons
         v->models.emplace(key, m);
     }
     return GS_OK;
+}
+
+gs_status gs_multi_viewer_insert_model(gs_multi_viewer *v, const char *key, const void *host, uint32_t count,
+                                       uint32_t format) {
+    if (!v || !key) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    Model *m = new Model();
+    const gs_status s = m->create(host, count, format);
+    if (s != GS_OK) {
+        delete m;
+        return s;
+    }
+    return multi_insert(v, key, m);
+}
+
+gs_status gs_multi_viewer_insert_model_from_ply(gs_multi_viewer *v, const char *key, const void *ply_bytes,
+                                                size_t len, uint32_t format) {
+    if (!v || !key || !ply_bytes) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    Model *m = new Model();
+    const gs_status s = m->create_from_ply(ply_bytes, len, format);
+    if (s != GS_OK) {
+        delete m;
+        return s;
+    }
+    return multi_insert(v, key, m);
 }
 
 gs_status gs_multi_viewer_remove_model(gs_multi_viewer *v, const char *key) {

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "gs_common.cuh"
+#include "gs_convert.cuh"
 #include "gs300.h"
 #include "gs_record.h"
 
@@ -36,6 +37,11 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
                               uint32_t *dispatch, uint32_t *indices, float *depths,
                               uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st,
                               const gs_frame_uniforms *u_dev = nullptr);
+
+// ---- PLY ingest (gs_ply.cu) ----
+gs_status ply_check_layout(const gs_ply_layout *layout);
+cudaError_t launch_ply_convert(const void *vertices, const gs_ply_layout &layout, uint32_t format, void *records,
+                               cudaStream_t st);
 
 // ---- K2 onesweep radix sort (gs_sort.cu) ----
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits);

@@ -37,6 +37,7 @@ __all__ = [
     "Camera", "CameraPod", "GaussianTransformPod", "ModelTransformPod", "FrameUniforms", "Viewer",
     "MultiModelViewer", "RenderTarget", "Preprocessor", "RadixSorter", "Renderer", "GsError",
     "ModelNotFound", "GaussianDisplayMode", "pack_gaussians", "frame_uniforms", "Batch", "Server",
+    "ply_parse_header", "ply_convert",
 ]
 
 
@@ -166,6 +167,27 @@ def _as_records(gaussians, fmt=None):
     raise GsError(1, f"unsupported Gaussian array dtype {a.dtype}")
 
 
+def _file_bytes(path_or_bytes):
+    if isinstance(path_or_bytes, (bytes, bytearray)):
+        return bytes(path_or_bytes)
+    with open(path_or_bytes, "rb") as f:
+        return f.read()
+
+
+def ply_parse_header(path_or_bytes):
+    """gs_ply_parse_header: the PlyLayout (field offsets, count, stride) of a PLY file."""
+    data = _file_bytes(path_or_bytes)
+    layout = records.PlyLayout()
+    check(lib().gs_ply_parse_header(data, len(data), ctypes.byref(layout)))
+    return layout
+
+
+def ply_convert(vertices_ptr, layout, fmt, records_ptr, stream=None):
+    """gs_ply_convert: device vertex block -> device records of `fmt` (asynchronous)."""
+    check(lib().gs_ply_convert(ctypes.c_void_p(vertices_ptr), ctypes.byref(layout), int(fmt),
+                               ctypes.c_void_p(records_ptr), _stream(stream)))
+
+
 class RenderTarget:
     """Headless Rgba8Unorm render target (≙ wgpu::Texture + TextureView)."""
 
@@ -218,6 +240,18 @@ class Viewer:
         check(lib().gs_viewer_create(recs.ctypes.data_as(ctypes.c_void_p), len(recs), f, ctypes.byref(h)))
         self._h = h
         self.format = f
+
+    @classmethod
+    def from_ply(cls, path_or_bytes, fmt=FORMAT_FP32):
+        """Viewer::new over Gaussians::read_from_file(path, GaussiansSource::Ply): the header is
+        scanned on the host, the vertex block converted into `fmt` records on the GPU."""
+        data = _file_bytes(path_or_bytes)
+        self = cls.__new__(cls)
+        h = ctypes.c_void_p()
+        check(lib().gs_viewer_create_from_ply(data, len(data), int(fmt), ctypes.byref(h)))
+        self._h = h
+        self.format = int(fmt)
+        return self
 
     def __len__(self):
         return lib().gs_viewer_len(self._h)
@@ -290,6 +324,10 @@ class MultiModelViewer:
     def insert_model(self, key, gaussians, fmt=None):
         recs, f = _as_records(gaussians, fmt)
         check(lib().gs_multi_viewer_insert_model(self._h, key.encode(), recs.ctypes.data_as(ctypes.c_void_p), len(recs), f))
+
+    def insert_model_from_ply(self, key, path_or_bytes, fmt=FORMAT_FP32):
+        data = _file_bytes(path_or_bytes)
+        check(lib().gs_multi_viewer_insert_model_from_ply(self._h, key.encode(), data, len(data), int(fmt)))
 
     def remove_model(self, key):
         check(lib().gs_multi_viewer_remove_model(self._h, key.encode()))

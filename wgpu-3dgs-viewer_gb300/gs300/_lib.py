@@ -52,6 +52,8 @@ SIGNATURES = [
     ("gs_gaussian_transform_pod_new", ST, [F32, U32, U32, I32, F32, P]),
     ("gs_model_transform_pod_new", ST, [P, P, P, P]),
     ("gs_gaussian_pack", ST, [P, SZ, P]),
+    ("gs_ply_parse_header", ST, [P, SZ, P]),
+    ("gs_ply_convert", ST, [P, P, U32, P, P]),
     ("gs_frame_uniforms_build", ST, [P, P, P, U32, U32, P]),
     ("gs_depth_capacity", U32, [U32]),
     ("gs_preprocess_scratch_bytes", SZ, [U32]),
@@ -63,6 +65,7 @@ SIGNATURES = [
     ("gs_rasterize", ST, [P, P, P, P, U32, P, U32, U32, U32, U32, P, SZ, P]),
     ("gs_scratch_status", ST, [P, P, ctypes.POINTER(U32)]),
     ("gs_viewer_create", ST, [P, U32, U32, PP]),
+    ("gs_viewer_create_from_ply", ST, [P, SZ, U32, PP]),
     ("gs_viewer_destroy", None, [P]),
     ("gs_viewer_len", U32, [P]),
     ("gs_viewer_update_camera", ST, [P, P, U32, U32]),
@@ -84,6 +87,7 @@ SIGNATURES = [
     ("gs_multi_viewer_create", ST, [PP]),
     ("gs_multi_viewer_destroy", None, [P]),
     ("gs_multi_viewer_insert_model", ST, [P, CP, P, U32, U32]),
+    ("gs_multi_viewer_insert_model_from_ply", ST, [P, CP, P, SZ, U32]),
     ("gs_multi_viewer_remove_model", ST, [P, CP]),
     ("gs_multi_viewer_model_count", U32, [P]),
     ("gs_multi_viewer_update_camera", ST, [P, P, U32, U32]),

@@ -19,7 +19,7 @@ CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 BUILD_DIR = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libgs300.so")
-SOURCES = ["gs_api.cu", "gs_preprocess.cu", "gs_sort.cu", "gs_raster.cu"]
+SOURCES = ["gs_api.cu", "gs_preprocess.cu", "gs_sort.cu", "gs_raster.cu", "gs_ply.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

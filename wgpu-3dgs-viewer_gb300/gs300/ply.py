@@ -5,7 +5,8 @@ The reference loads scenes through the un-vendored wgpu-3dgs-core 0.6.0 PLY read
 (examples/simple.rs:156-160); its fixture is coverage/model.ply.  This module follows the
 published convention of that format:
   * colour rgb = 0.5 + SH_C0 · f_dc (clamped, rounded to 8 bits), alpha = sigmoid(opacity);
-  * f_rest is stored channel-major (15 coefficients of R, then G, then B);
+  * f_rest is stored channel-major (K coefficients of R, then G, then B; K = 3, 8 or 15 for SH
+    degree 1, 2 or 3, the missing bands zero);
   * scale = exp(scale_i); rotation is stored (w, x, y, z) and normalised.
 The conversion constants are this library's own choice where the crate is unpinned.
 """
@@ -29,28 +30,32 @@ def parse_header(data):
         raise ValueError("not a PLY file")
     lines = data[:end].decode("ascii").splitlines()
     fmt = None
-    count = None
-    fields = []
-    in_vertex = False
+    elements = []  # [name, count, [(field, type)], has_list]
     for ln in lines[1:]:
         parts = ln.split()
-        if not parts:
+        if not parts or parts[0] in ("comment", "obj_info"):
             continue
         if parts[0] == "format":
             fmt = parts[1]
         elif parts[0] == "element":
-            in_vertex = parts[1] == "vertex"
-            if in_vertex:
-                count = int(parts[2])
-        elif parts[0] == "property" and in_vertex:
+            elements.append([parts[1], int(parts[2]), [], False])
+        elif parts[0] == "property":
             if parts[1] == "list":
-                raise ValueError("list properties are not supported in the vertex element")
-            fields.append((parts[2], _TYPES[parts[1]]))
+                if elements[-1][0] == "vertex":
+                    raise ValueError("list properties are not supported in the vertex element")
+                elements[-1][3] = True
+            else:
+                elements[-1][2].append((parts[2], _TYPES[parts[1]]))
     if fmt != "binary_little_endian":
         raise ValueError(f"unsupported PLY format {fmt}")
-    if count is None:
-        raise ValueError("PLY has no vertex element")
-    return count, np.dtype(fields), end + len(b"end_header\n")
+    offset = end + len(b"end_header\n")
+    for name, count, fields, has_list in elements:
+        if name == "vertex":
+            return count, np.dtype(fields), offset
+        if has_list:
+            raise ValueError(f"element {name} before the vertex element has a list property")
+        offset += count * np.dtype(fields).itemsize
+    raise ValueError("PLY has no vertex element")
 
 
 def read_vertices(path_or_bytes):
@@ -70,10 +75,15 @@ def vertices_to_gaussians(v):
     out["color"][:, :3] = np.rint(rgb * 255.0).astype(np.uint8)
     out["color"][:, 3] = np.rint(op * 255.0).astype(np.uint8)
     names = v.dtype.names
-    rest = [f"f_rest_{i}" for i in range(45)]
-    if all(r in names for r in rest):
-        fr = np.stack([v[r] for r in rest], axis=1).reshape(n, 3, 15)  # [channel][coefficient]
-        out["sh"] = np.transpose(fr, (0, 2, 1)).reshape(n, 45)
+    m = sum(1 for r in names if r.startswith("f_rest_"))
+    if m not in (0, 9, 24, 45):
+        raise ValueError(f"PLY f_rest count must be 0, 9, 24 or 45, not {m}")
+    if m:
+        k = m // 3  # coefficients per channel; bands above the file's degree stay zero
+        fr = np.stack([v[f"f_rest_{i}"] for i in range(m)], axis=1).reshape(n, 3, k)  # [channel][coefficient]
+        sh = np.zeros((n, 15, 3), dtype=np.float32)
+        sh[:, :k, :] = np.transpose(fr, (0, 2, 1))
+        out["sh"] = sh.reshape(n, 45)
     out["scale"] = np.exp(np.stack([v[f"scale_{i}"] for i in range(3)], axis=1).astype(np.float64))
     q = np.stack([v["rot_1"], v["rot_2"], v["rot_3"], v["rot_0"]], axis=1).astype(np.float64)
     q /= np.linalg.norm(q, axis=1, keepdims=True)

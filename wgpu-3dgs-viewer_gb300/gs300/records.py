@@ -49,6 +49,23 @@ SPLAT_DTYPE = np.dtype(
 assert SPLAT_DTYPE.itemsize == 48
 
 
+class PlyLayout(ctypes.Structure):
+    """gs_ply_layout: where the fields of one PLY vertex lie (byte offsets; -1 = absent)."""
+
+    _fields_ = [
+        ("data_offset", ctypes.c_uint64),
+        ("count", ctypes.c_uint32),
+        ("stride", ctypes.c_uint32),
+        ("sh_rest", ctypes.c_uint32),
+        ("pos", ctypes.c_int32 * 3),
+        ("f_dc", ctypes.c_int32 * 3),
+        ("opacity", ctypes.c_int32),
+        ("scale", ctypes.c_int32 * 3),
+        ("rot", ctypes.c_int32 * 4),
+        ("f_rest", ctypes.c_int32 * 45),
+    ]
+
+
 class Camera(ctypes.Structure):
     """gs_camera (src/camera.rs:16-29)."""
 

@@ -64,6 +64,24 @@ def pack_gaussians(gaussians):
     return out
 
 
+def pack_gaussians_half(gaussians, fmt):
+    """core::Gaussian records -> gs_gaussian_pod_half records (rotation, scale to binary16; SH to
+    binary16 or bfloat16; round to nearest even)."""
+    g = np.asarray(gaussians, dtype=GAUSSIAN_DTYPE)
+    out = np.zeros(g.shape, dtype=GAUSSIAN_POD_HALF_DTYPE)
+    out["pos"] = g["pos"]
+    out["color"] = pack_color(g["color"])
+    out["rot"] = g["rot"].astype(np.float16).view(np.uint16)
+    out["scale"] = g["scale"].astype(np.float16).view(np.uint16)
+    if fmt == FORMAT_HALF_SH_FP16:
+        out["sh"] = g["sh"].astype(np.float16).view(np.uint16)
+    elif fmt == FORMAT_HALF_SH_BF16:
+        out["sh"] = _f32_to_bf16_bits(g["sh"])
+    else:
+        raise ValueError(f"not a half record format: {fmt}")
+    return out
+
+
 def gaussian(pos=(0.0, 0.0, 1.0), rot=(0.0, 0.0, 0.0, 1.0), color=(255, 0, 0, 255), scale=(1.0, 1.0, 1.0), sh=None):
     """One core::Gaussian, defaulting to the reference tests' red Gaussian (tests/e2e/viewer.rs:74-80)."""
     g = np.zeros((), dtype=GAUSSIAN_DTYPE)
