@@ -565,6 +565,10 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
             end = base;
         }
         if (!found) k = 0;
+        // The bounds argument holds from any start position, so a warp starts all its pixels at
+        // the smallest k among them: lanes share issue slots, the earlier start costs the warp
+        // nothing, and it makes the bounds more likely to meet on the first pass.
+        k = __reduce_min_sync(0xFFFFFFFFu, k);
         // ---- B: bounded back-to-front passes from k ----
         bool active = true;
         float h0 = 0.0f, h1 = 0.0f, h2 = 0.0f;
@@ -586,11 +590,12 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
                 __syncthreads();
                 stage_chunk<MODE>(S, sorted, pairs, s0 + base, cnt, std2, max_splats);
                 __syncthreads();
-                if (__any_sync(0xFFFFFFFFu, active)) {
+                // k is uniform across the warp: a warp whose suffix starts past this chunk skips it
+                const bool inside = active && k < base + kRasterThreads;  // chunk holds suffix entries
+                if (__any_sync(0xFFFFFFFFu, inside)) {
                     const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
                     // Bounds that have met stay equal (same inputs, same operations), so once
                     // every started lane of the warp has met, one chain per channel suffices.
-                    const bool inside = active && k < base + kRasterThreads;  // chunk holds suffix entries
                     const bool met = d0 == h0 && d1 == h1 && d2 == h2;
                     if (__all_sync(0xFFFFFFFFu, !inside || (met && base >= k))) {
                         for (uint32_t i = 0; i < nl; ++i) {
