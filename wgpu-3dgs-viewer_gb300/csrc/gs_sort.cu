@@ -167,7 +167,10 @@ __device__ __forceinline__ uint32_t look_back_digit(const uint64_t *flags, uint3
 // One LSD pass over the digit at `shift`.  Input and output are either split (keys[],
 // values[]) or packed (uint2 {key, value}); packed ping-pong buffers keep each digit's run of
 // 8-byte pairs contiguous in the scatter.
-template <bool IN_PACKED, bool OUT_PACKED>
+// MATCH: peers from one match.any instead of a ballot per digit bit.  Measured on GB300, match.any
+// is the cheaper of the two for depth keys (digits spread over many values) and the dearer for
+// tile keys (few distinct digits per warp, and 5 live bits in the last pass).
+template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
 __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
@@ -208,18 +211,23 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
             k[i] = ok ? kin[pos] : 0xFFFFFFFFu;
         }
     }
-    // Warp-local stable ranking: lanes that share a digit form a peer mask from 8 ballots.
+    // Warp-local stable ranking: lanes that share a digit form a peer mask (match.any, or one
+    // ballot per live digit bit).
     const uint32_t lt = lanemask_lt();
 #pragma unroll
     for (uint32_t i = 0; i < kSortRows; ++i) {
         const uint32_t d = (k[i] >> shift) & dmask;
         uint32_t peers = 0xFFFFFFFFu;
+        if constexpr (MATCH) {
+            peers = __match_any_sync(0xFFFFFFFFu, d);
+        } else {
 #pragma unroll
-        for (uint32_t b = 0; b < 8; ++b) {
-            if (b >= digit_bits) break;  // bits above the key width are zero in every key
-            const uint32_t bit = (d >> b) & 1u;
-            const uint32_t bal = __ballot_sync(0xFFFFFFFFu, bit);
-            peers &= bit ? bal : ~bal;
+            for (uint32_t b = 0; b < 8; ++b) {
+                if (b >= digit_bits) break;  // bits above the key width are zero in every key
+                const uint32_t bit = (d >> b) & 1u;
+                const uint32_t bal = __ballot_sync(0xFFFFFFFFu, bit);
+                peers &= bit ? bal : ~bal;
+            }
         }
         const uint32_t rank = __popc(peers & lt);
         const uint32_t pre = s_whist[warp][d];
@@ -373,24 +381,24 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     count_launches(1);
     const size_t fstride = (size_t)L.ntiles * 256;
     if (npasses == 1) {
-        sort_pass_kernel<false, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, L.alt_a,
+        sort_pass_kernel<false, true, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, L.alt_a,
                                                                         count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
         unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
         count_launches(2);
     } else {
         uint2 *src = L.alt_a, *dst = L.alt_b;
-        sort_pass_kernel<false, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, src,
+        sort_pass_kernel<false, true, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, src,
                                                                         count, max_count, 0, pass_bits(key_bits, 0),
                                                                         L.ctrl, L.flags);
         for (uint32_t p = 1; p + 1 < npasses; ++p) {
-            sort_pass_kernel<true, true><<<L.ntiles, kSortThreads, 0, st>>>(
+            sort_pass_kernel<true, true, true><<<L.ntiles, kSortThreads, 0, st>>>(
                 nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, pass_bits(key_bits, p), L.ctrl,
                 L.flags + p * fstride);
             uint2 *t = src;
             src = dst;
             dst = t;
         }
-        sort_pass_kernel<true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, keys, vals, nullptr, count,
+        sort_pass_kernel<true, false, true><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, keys, vals, nullptr, count,
                                                                         max_count, npasses - 1,
                                                                         pass_bits(key_bits, npasses - 1), L.ctrl,
                                                                         L.flags + (npasses - 1) * fstride);
@@ -416,7 +424,7 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
     const size_t fstride = (size_t)L.ntiles * 256;
     uint2 *src = data, *dst = L.alt_a;
     for (uint32_t p = 0; p < npasses; ++p) {
-        sort_pass_kernel<true, true><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
+        sort_pass_kernel<true, true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
                                                                        count, max_count, p, pass_bits(key_bits, p), L.ctrl,
                                                                        L.flags + p * fstride);
         uint2 *t = src;
