@@ -5,6 +5,7 @@ with new cameras."""
 import numpy as np
 import pytest
 
+from gs300 import records as R
 from gs300 import scene as S
 
 pytestmark = pytest.mark.gpu
@@ -12,8 +13,8 @@ pytestmark = pytest.mark.gpu
 SIZES = [(640, 360), (1280, 720), (333, 197), (1920, 1080)]
 
 
-def _single(gs, records, mt, cam, w, h):
-    v = gs.Viewer(records)
+def _single(gs, records, mt, cam, w, h, fmt=None):
+    v = gs.Viewer(records, fmt)
     v.update_model_transform_with_pod(mt)
     v.update_camera(cam, (w, h))
     t = gs.RenderTarget(w, h)
@@ -56,3 +57,37 @@ def test_batch_reports_missing_model(gs, cuda):
         batch.render([("b", pod, t)])
     batch.render([("a", pod, t)])
     batch.synchronize()
+
+
+def test_batch_shared_record_reads(gs, cuda, monkeypatch):
+    """Views of one model share one preprocess launch (records read once, up to 16 views per
+    launch): 20 views of a half-record model make two launches (16 + 4), interleaved with views
+    of an FP32 model and of an empty model; every view equals its single-view render."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    scenes = {"half": (S.synth_scene(50_000, seed=7, fmt=R.FORMAT_HALF_SH_BF16), R.FORMAT_HALF_SH_BF16),
+              "fp32": (S.synth_scene(20_000, seed=8), None),
+              "empty": (S.synth_scene(0, seed=9), None)}
+    mv = gs.MultiModelViewer()
+    for k, (sc, fmt) in scenes.items():
+        mv.insert_model(k, sc, fmt)
+    keys = list(scenes)
+    batch = gs.Batch(mv, keys)
+    plan = []
+    for i in range(20):
+        plan.append(("half", (320 + 16 * (i % 3), 180)))
+        if i % 7 == 3:
+            plan.append(("fp32", (256, 144)))
+    plan.insert(5, ("empty", (64, 48)))
+    targets = [gs.RenderTarget(w, h) for _, (w, h) in plan]
+    mt = gs.model_transform_pod()
+    for call in range(2):
+        cams = [S.orbit_camera(3 * j + 17 * call, radius=6.0 + 0.1 * j) for j in range(len(plan))]
+        batch.render([(k, gs.CameraPod.new(c, wh), t) for (k, wh), c, t in zip(plan, cams, targets)])
+        batch.synchronize()
+        for (k, (w, h)), cam, t in zip(plan, cams, targets):
+            sc, fmt = scenes[k]
+            got = t.download()
+            if k == "empty":
+                assert (got[..., :3] == 0).all() and (got[..., 3] == 255).all()
+                continue
+            assert np.array_equal(got, _single(gs, sc, mt, cam, w, h, fmt))

@@ -1058,6 +1058,10 @@ struct gs_batch {
     uint32_t uniforms_cap = 0;
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
+    std::vector<cudaEvent_t> chunk_events;  // one per multi-view preprocess launch
+    DevBuf views_dev;                       // PreView per view (device), rebuilt with the graph
+    DevBuf group_dev;                       // one control block per multi-view launch
+    uint32_t chunks = 0;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::string shape;
@@ -1069,6 +1073,7 @@ struct gs_batch {
         if (exec) cudaGraphExecDestroy(exec);
         for (auto s : streams) cudaStreamDestroy(s);
         for (auto e : events) cudaEventDestroy(e);
+        for (auto e : chunk_events) cudaEventDestroy(e);
         if (capture) cudaStreamDestroy(capture);
         if (uniforms_host) cudaFreeHost(uniforms_host);
     }
@@ -1125,29 +1130,83 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
             b->events.push_back(e);
         }
         const uint32_t nstreams = n < kBatchStreams ? n : kBatchStreams;
+        // Views of one model share its record reads: one preprocess launch per chunk of up to
+        // kPreMaxViews views of the same model, in order of first appearance.
+        std::vector<std::vector<uint32_t>> chunks;
+        {
+            std::vector<const Model *> seen;
+            std::vector<std::vector<uint32_t>> by_model;
+            for (uint32_t i = 0; i < n; ++i) {
+                size_t g = 0;
+                while (g < seen.size() && seen[g] != ms[i]) ++g;
+                if (g == seen.size()) {
+                    seen.push_back(ms[i]);
+                    by_model.emplace_back();
+                }
+                by_model[g].push_back(i);
+            }
+            for (auto &grp : by_model)
+                for (size_t k = 0; k < grp.size(); k += kPreMaxViews)
+                    chunks.emplace_back(grp.begin() + k, grp.begin() + std::min(grp.size(), k + kPreMaxViews));
+        }
+        const gs_frame_uniforms *udev = reinterpret_cast<const gs_frame_uniforms *>(b->uniforms_dev.ptr);
+        std::vector<PreView> pv(n);
+        std::vector<uint32_t> slot_of(n);  // position of view i in the PreView array
+        {
+            uint32_t at = 0;
+            for (auto &ch : chunks)
+                for (uint32_t i : ch) {
+                    ViewSlot &v = b->slots[i];
+                    uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+                    pv[at] = preprocess_view(udev + i, ind, ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr,
+                                             gs_depth_capacity(ms[i]->n), (gs_splat *)v.splats.ptr, v.pre_scratch.ptr);
+                    slot_of[i] = at++;
+                }
+        }
+        GS_CUDA(b->views_dev.ensure((size_t)n * sizeof(PreView)));
+        GS_CUDA(cudaMemcpy(b->views_dev.ptr, pv.data(), (size_t)n * sizeof(PreView), cudaMemcpyHostToDevice));
+        const size_t gbytes = align_up(sizeof(Ctrl), 256);
+        if (b->group_dev.bytes < chunks.size() * gbytes) {
+            GS_CUDA(b->group_dev.ensure(chunks.size() * gbytes));
+            GS_CUDA(cudaMemset(b->group_dev.ptr, 0, chunks.size() * gbytes));
+        }
+        while (b->chunk_events.size() < chunks.size()) {
+            cudaEvent_t e;
+            GS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            b->chunk_events.push_back(e);
+        }
+        b->chunks = (uint32_t)chunks.size();
+        const PreView *pv_dev = reinterpret_cast<const PreView *>(b->views_dev.ptr);
         GS_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
         t_capturing = true;
         t_captured_launches = 0;
         cudaError_t err = cudaEventRecord(b->events[kBatchStreams], b->capture);
         for (uint32_t s = 0; s < nstreams && err == cudaSuccess; ++s)
             err = cudaStreamWaitEvent(b->streams[s], b->events[kBatchStreams], 0);
-        const gs_frame_uniforms *udev = reinterpret_cast<const gs_frame_uniforms *>(b->uniforms_dev.ptr);
-        for (uint32_t i = 0; i < n && err == cudaSuccess; ++i) {
-            ViewSlot &v = b->slots[i];
-            const Model *m = ms[i];
-            cudaStream_t vs = b->streams[i % nstreams];
-            uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
-            err = launch_preprocess(b->uniforms_host[i], m->records.ptr, m->format, m->n,
-                                    m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert, ind,
-                                    ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr, gs_depth_capacity(m->n),
-                                    (gs_splat *)v.splats.ptr, v.pre_scratch.ptr, vs, udev + i);
-            if (err == cudaSuccess)
-                err = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, 32,
-                                  v.sort_scratch.ptr, vs);
-            if (err == cudaSuccess) {
-                const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
-                err = launch_raster(&seg, 1, b->uniforms_host[i], views[i].target, views[i].width, views[i].height,
-                                    views[i].pitch, v.max_pairs, v.raster_scratch.ptr, mv->frame.exact_exp, vs);
+        for (size_t c = 0; c < chunks.size() && err == cudaSuccess; ++c) {
+            const Model *m = ms[chunks[c][0]];
+            cudaStream_t cs = b->streams[c % nstreams];
+            err = launch_preprocess_views(m->records.ptr, m->format, m->n,
+                                          m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert,
+                                          pv_dev + slot_of[chunks[c][0]], (uint32_t)chunks[c].size(),
+                                          (uint8_t *)b->group_dev.ptr + c * gbytes, cs);
+            if (err == cudaSuccess) err = cudaEventRecord(b->chunk_events[c], cs);
+            for (uint32_t i : chunks[c]) {
+                if (err != cudaSuccess) break;
+                ViewSlot &v = b->slots[i];
+                cudaStream_t vs = b->streams[i % nstreams];
+                uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+                if (vs != cs) err = cudaStreamWaitEvent(vs, b->chunk_events[c], 0);
+                if (err == cudaSuccess)
+                    err = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, ms[i]->n, ind + 1, 32,
+                                      v.sort_scratch.ptr, vs);
+                if (err == cudaSuccess) {
+                    const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1,
+                                            ms[i]->n};
+                    err = launch_raster(&seg, 1, b->uniforms_host[i], views[i].target, views[i].width,
+                                        views[i].height, views[i].pitch, v.max_pairs, v.raster_scratch.ptr,
+                                        mv->frame.exact_exp, vs);
+                }
             }
         }
         for (uint32_t s = 0; s < nstreams && err == cudaSuccess; ++s) {
@@ -1216,7 +1275,14 @@ gs_status gs_batch_synchronize(gs_batch *b, gs_stream stream) {
             GS_CUDA(cudaMemcpy(&c, v.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
             GS_CUDA(cudaMemcpy(&a, v.pre_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
             GS_CUDA(cudaMemcpy(&s, v.sort_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
-            const uint32_t bits = c.status | a.status | s.status;
+            uint32_t bits = c.status | a.status | s.status;
+            if (i == 0)
+                for (uint32_t k = 0; k < b->chunks; ++k) {
+                    Ctrl gc{};
+                    GS_CUDA(cudaMemcpy(&gc, (uint8_t *)b->group_dev.ptr + k * align_up(sizeof(Ctrl), 256), sizeof(Ctrl),
+                                       cudaMemcpyDeviceToHost));
+                    bits |= gc.status;
+                }
             if (bits & kStatusTimeout) return status_from_bits(bits, "batch");
             if (bits & kStatusCapacity) {
                 uint64_t p = (uint64_t)c.total + c.total / 4 + 4096;

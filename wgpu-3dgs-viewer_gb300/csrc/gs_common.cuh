@@ -32,6 +32,30 @@ struct Ctrl {
 };
 static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl must keep 16-byte alignment of what follows");
 
+// Resets a control block (one CTA): mode 1 = a new stage call (epoch, status, tickets, counters,
+// histograms); mode 0 = a new segment inside a call (epoch and tickets 0..1 only).  The epoch
+// tags every look-back flag, so flags of earlier calls never need clearing.
+__device__ __forceinline__ void ctrl_reset(Ctrl *ctrl, int mode) {
+    const uint32_t t = threadIdx.x;
+    if (t == 0) {
+        uint32_t e = ctrl->epoch + 1u;
+        if (e >= (1u << 30) || e == 0u) e = 1u;
+        ctrl->epoch = e;
+        ctrl->ticket[0] = 0u;
+        ctrl->ticket[1] = 0u;
+        if (mode == 1) {
+            ctrl->status = 0u;
+            for (int k = 1; k < 8; ++k) ctrl->ticket[k] = 0u;
+            ctrl->count = 0u;
+            ctrl->total = 0u;
+            ctrl->pair_base = 0u;
+            ctrl->seg_total = 0u;
+        }
+    }
+    if (mode == 1)
+        for (uint32_t k = t; k < 4 * 256; k += blockDim.x) (&ctrl->hist[0][0])[k] = 0u;
+}
+
 // Look-back flag word: epoch (30 bits) | status (2 bits) | value (32 bits).
 constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;

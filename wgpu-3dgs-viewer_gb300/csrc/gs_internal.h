@@ -38,6 +38,26 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
                               uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st,
                               const gs_frame_uniforms *u_dev = nullptr);
 
+// Several views of one model in one launch (records read once).  A view's scratch is the one
+// launch_preprocess takes for that model; `group` is a zeroed Ctrl-sized block for the launch.
+struct PreView {
+    const gs_frame_uniforms *u;  // device
+    uint32_t *indirect;
+    uint32_t *dispatch;
+    uint32_t *indices;
+    float *depths;
+    uint32_t depth_cap;
+    gs_splat *splats;
+    Ctrl *ctrl;
+    uint64_t *flags;
+};
+constexpr uint32_t kPreMaxViews = 16;
+PreView preprocess_view(const gs_frame_uniforms *u_dev, uint32_t *indirect, uint32_t *dispatch, uint32_t *indices,
+                        float *depths, uint32_t depth_cap, gs_splat *splats, void *scratch);
+cudaError_t launch_preprocess_views(const void *records, uint32_t format, uint32_t n, const uint32_t *selection,
+                                    int invert, const PreView *views_dev, uint32_t nviews, void *group,
+                                    cudaStream_t st);
+
 // ---- PLY ingest (gs_ply.cu) ----
 gs_status ply_check_layout(const gs_ply_layout *layout);
 cudaError_t launch_ply_convert(const void *vertices, const gs_ply_layout &layout, uint32_t format, void *records,

@@ -38,6 +38,17 @@ struct PreParams {
     uint64_t *flags;
 };
 
+struct PreViewsParams {
+    const uint8_t *records;
+    uint32_t n;
+    uint32_t ntiles;
+    const uint32_t *selection;
+    uint32_t invert;
+    const PreView *views;  // device array of nviews
+    uint32_t nviews;
+    Ctrl *group;           // tile tickets of the launch (status of the record staging)
+};
+
 // ---- FP32 math in the oracle's evaluation order ------------------------------------------
 __device__ __forceinline__ void mat4_vec(const float *m, const float *v, float *o) {
 #pragma unroll
@@ -305,6 +316,106 @@ __device__ __forceinline__ void view_color(const gs_frame_uniforms &u, const Rec
     rgba[3] = (float)((g.color >> 24) & 0xFFu) / 255.0f;
 }
 
+// ---- per Gaussian and view -------------------------------------------------------------------
+// Projection state of one Gaussian in one view, carried from the cull to the splat record.
+struct Proj {
+    float nx, ny, world[4], axes[4];
+    bool have_axes;
+};
+
+// `main` (preprocess.wesl:60-106): NDC cull, then the bound cull along the major axis for
+// centres outside the frustum.  Returns visibility; *key = 1 - ndc.z.
+__device__ __forceinline__ bool gaussian_visible(const gs_frame_uniforms &u, const Rec &g, Proj &pr, float *key) {
+    const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], 1.0f};
+    float clip[4];
+    mat4_vec(u.model, p4, pr.world);
+    mat4_vec(u.pv, pr.world, clip);
+    pr.nx = clip[0] / clip[3];
+    pr.ny = clip[1] / clip[3];
+    const float nz = clip[2] / clip[3];
+    pr.have_axes = false;
+    bool vis = true;
+    if (cull(pr.nx, pr.ny, nz)) {
+        cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, pr.axes);
+        pr.have_axes = true;
+        const float mx = pr.axes[0] * u.std_dev / u.size[0];
+        const float my = pr.axes[1] * u.std_dev / u.size[1];
+        const float mlen = len2(mx, my);
+        const float nl = len2(pr.nx, pr.ny);
+        const float dx = -pr.nx / nl, dy = -pr.ny / nl;
+        const float m = minf_wgsl(mlen, nl);
+        if (cull(pr.nx + m * dx, pr.ny + m * dy, nz)) vis = false;
+    }
+    *key = 1.0f - nz;
+    return vis;
+}
+
+// Per-instance vertex work (render.wesl:75-130): the splat record of a visible Gaussian.
+template <uint32_t FMT>
+__device__ __forceinline__ void write_splat(const gs_frame_uniforms &u, const Rec &g, Proj &pr, gs_splat *out) {
+    float rgba[4];
+    view_color<FMT>(u, g, pr.world, rgba);
+    const float W = u.viewport[0], H = u.viewport[1];
+    const float cx = ((pr.nx + 1.0f) * W) * 0.5f;
+    const float cy = ((1.0f - pr.ny) * H) * 0.5f;
+    float q0, q1, q2, q3, ex, ey;
+    const float std2 = u.std_dev * u.std_dev;
+    const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], 1.0f};
+    if (u.display_mode == GS_DISPLAY_POINT) {
+        float vp[4];
+        mat4_vec(u.vm, p4, vp);
+        const float l = sqrtf((vp[0] * vp[0] + vp[1] * vp[1]) + vp[2] * vp[2]);
+        const float aspect = u.size[1] / u.size[0];
+        const float pnd = (0.01f * u.point_size) / l;
+        const float hx = (pnd * aspect) * (0.5f * W);
+        const float hy = pnd * (0.5f * H);
+        q0 = hx;
+        q1 = hy;
+        q2 = 0.0f;
+        q3 = 0.0f;
+        if (hx > 0.0f && hy > 0.0f && hx < 1e30f && hy < 1e30f) {
+            ex = hx * 1.001f + 0.01f;
+            ey = hy * 1.001f + 0.01f;
+        } else {
+            ex = -1.0f;
+            ey = -1.0f;
+        }
+    } else {
+        if (!pr.have_axes) cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, pr.axes);
+        const float *axes = pr.axes;
+        const float kx = (0.5f * W) / u.size[0];
+        const float ky = (0.5f * H) / u.size[1];
+        const float a00 = axes[0] * kx, a01 = axes[2] * kx;
+        const float a10 = -axes[1] * ky, a11 = -axes[3] * ky;
+        const float det = a00 * a11 - a01 * a10;
+        q0 = a11 / det;
+        q1 = -a01 / det;
+        q2 = -a10 / det;
+        q3 = a00 / det;
+        const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
+        const bool ok = det != 0.0f && isfinite(det) && isfinite(q0) && isfinite(q1) && isfinite(q2) &&
+                        isfinite(q3) && r2 >= 0.0f;
+        if (ok) {
+            ex = sqrtf(r2 * (a00 * a00 + a01 * a01)) * 1.001f + 0.01f;
+            ey = sqrtf(r2 * (a10 * a10 + a11 * a11)) * 1.001f + 0.01f;
+        } else {
+            ex = -1.0f;
+            ey = -1.0f;
+        }
+    }
+    float4 *sp = reinterpret_cast<float4 *>(out);
+    sp[0] = make_float4(cx, cy, ex, ey);
+    sp[1] = make_float4(q0, q1, q2, q3);
+    sp[2] = make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f, rgba[3]);
+}
+
+// Selection (preprocess.wesl:68-78): a Gaussian takes part when its bit differs from `invert`.
+__device__ __forceinline__ bool gaussian_selected(const uint32_t *selection, uint32_t invert, uint32_t i) {
+    if (!selection) return true;
+    const bool bit = (selection[i >> 5] >> (i & 31u)) & 1u;
+    return (invert != 0u) != bit;
+}
+
 // ---- global -> shared staging: 16-byte cp.async chunks, or a bulk copy on an mbarrier -----
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
     const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
@@ -350,6 +461,40 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
+// Records [first, first + cnt) into shared rows: FP32 records by one bulk copy on the mbarrier
+// (phase 0, initialised by the caller before a __syncthreads), half records by 16-byte cp.async
+// chunks into padded rows.  Returns with the rows visible to every thread of the CTA.
+template <uint32_t FMT>
+__device__ __forceinline__ void stage_records(uint4 *s_rec, uint64_t *s_bar, const uint8_t *records, uint32_t first,
+                                              uint32_t cnt, uint32_t *status) {
+    constexpr uint32_t REC = (FMT == GS_FORMAT_FP32) ? 224u : 128u;
+    constexpr uint32_t C16 = REC / 16;
+    constexpr uint32_t ROW16 = (FMT == GS_FORMAT_FP32) ? C16 : C16 + 1;
+    const uint32_t tid = threadIdx.x;
+    if constexpr (FMT == GS_FORMAT_FP32) {
+        if (tid == 0) {
+            mbar_expect_tx(s_bar, cnt * REC);
+            bulk_g2s(s_rec, records + (size_t)first * REC, cnt * REC, s_bar);
+        }
+        if (!mbar_wait(s_bar, 0)) atomicOr(status, kStatusTimeout);
+    } else {
+        // consecutive threads copy consecutive 16-byte chunks (coalesced); chunk q of the CTA
+        // is chunk q % C16 of record q / C16
+        const uint4 *src = reinterpret_cast<const uint4 *>(records + (size_t)first * REC);
+        const uint32_t chunks = cnt * C16;
+#pragma unroll
+        for (uint32_t k = 0; k < C16; ++k) {
+            const uint32_t q = tid + k * kPreThreads;
+            if (q < chunks) {
+                const uint32_t r = q / C16;
+                cp_async16(&s_rec[r * ROW16 + (q - r * C16)], src + q);
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+    }
+}
+
 template <uint32_t FMT, bool DEV_UNIFORMS>
 __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_constant__ PreParams P) {
     constexpr uint32_t REC = (FMT == GS_FORMAT_FP32) ? 224u : 128u;
@@ -380,64 +525,16 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     const uint32_t tile = s_tile, epoch = s_epoch;
     const uint32_t first = tile * kPreThreads;
     const uint32_t cnt = min(kPreThreads, P.n - first);
-    if constexpr (BULK) {
-        if (tid == 0) {
-            mbar_expect_tx(&s_bar, cnt * REC);
-            bulk_g2s(s_rec, P.records + (size_t)first * REC, cnt * REC, &s_bar);
-        }
-        if (!mbar_wait(&s_bar, 0)) atomicOr(&P.ctrl->status, kStatusTimeout);
-    } else {
-        // consecutive threads copy consecutive 16-byte chunks (coalesced); chunk q of the CTA
-        // is chunk q % C16 of record q / C16
-        const uint4 *src = reinterpret_cast<const uint4 *>(P.records + (size_t)first * REC);
-        const uint32_t chunks = cnt * C16;
-#pragma unroll
-        for (uint32_t k = 0; k < C16; ++k) {
-            const uint32_t q = tid + k * kPreThreads;
-            if (q < chunks) {
-                const uint32_t r = q / C16;
-                cp_async16(&s_rec[r * ROW16 + (q - r * C16)], src + q);
-            }
-        }
-        cp_async_wait_all();
-        __syncthreads();
-    }
+    stage_records<FMT>(s_rec, &s_bar, P.records, first, cnt, &P.ctrl->status);
 
     const uint32_t i = first + tid;
     bool vis = false;
-    float key = 0.0f, nx = 0.0f, ny = 0.0f, world[4], axes[4];
-    bool have_axes = false;
+    float key = 0.0f;
+    Proj pr;
     Rec g;
-    const float p4w = 1.0f;
-    if (tid < cnt) {
-        bool selected = true;
-        if (P.selection) {
-            const bool bit = (P.selection[i >> 5] >> (i & 31u)) & 1u;
-            selected = (P.invert != 0u) != bit;
-        }
-        if (selected) {
-            g = load_rec<FMT>(s_rec + tid * ROW16);
-            const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
-            float clip[4];
-            mat4_vec(u.model, p4, world);
-            mat4_vec(u.pv, world, clip);
-            nx = clip[0] / clip[3];
-            ny = clip[1] / clip[3];
-            const float nz = clip[2] / clip[3];
-            vis = true;
-            if (cull(nx, ny, nz)) {
-                cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, axes);
-                have_axes = true;
-                const float mx = axes[0] * u.std_dev / u.size[0];
-                const float my = axes[1] * u.std_dev / u.size[1];
-                const float mlen = len2(mx, my);
-                const float nl = len2(nx, ny);
-                const float dx = -nx / nl, dy = -ny / nl;
-                const float m = minf_wgsl(mlen, nl);
-                if (cull(nx + m * dx, ny + m * dy, nz)) vis = false;
-            }
-            key = 1.0f - nz;
-        }
+    if (tid < cnt && gaussian_selected(P.selection, P.invert, i)) {
+        g = load_rec<FMT>(s_rec + tid * ROW16);
+        vis = gaussian_visible(u, g, pr, &key);
     }
 
     // ---- order-preserving compaction: ballot + block scan; the CTA's count is published now
@@ -457,62 +554,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     }
 
     // ---- per-instance vertex work (render.wesl:75-130), written at the Gaussian's index ----
-    if (vis && P.splats) {
-        float rgba[4];
-        view_color<FMT>(u, g, world, rgba);
-        const float W = u.viewport[0], H = u.viewport[1];
-        const float cx = ((nx + 1.0f) * W) * 0.5f;
-        const float cy = ((1.0f - ny) * H) * 0.5f;
-        float q0, q1, q2, q3, ex, ey;
-        const float std2 = u.std_dev * u.std_dev;
-        const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], p4w};
-        if (u.display_mode == GS_DISPLAY_POINT) {
-            float vp[4];
-            mat4_vec(u.vm, p4, vp);
-            const float l = sqrtf((vp[0] * vp[0] + vp[1] * vp[1]) + vp[2] * vp[2]);
-            const float aspect = u.size[1] / u.size[0];
-            const float pnd = (0.01f * u.point_size) / l;
-            const float hx = (pnd * aspect) * (0.5f * W);
-            const float hy = pnd * (0.5f * H);
-            q0 = hx;
-            q1 = hy;
-            q2 = 0.0f;
-            q3 = 0.0f;
-            if (hx > 0.0f && hy > 0.0f && hx < 1e30f && hy < 1e30f) {
-                ex = hx * 1.001f + 0.01f;
-                ey = hy * 1.001f + 0.01f;
-            } else {
-                ex = -1.0f;
-                ey = -1.0f;
-            }
-        } else {
-            if (!have_axes) cov2d_axes(u, g.cov3d, p4, u.std_dev_scaled, axes);
-            const float kx = (0.5f * W) / u.size[0];
-            const float ky = (0.5f * H) / u.size[1];
-            const float a00 = axes[0] * kx, a01 = axes[2] * kx;
-            const float a10 = -axes[1] * ky, a11 = -axes[3] * ky;
-            const float det = a00 * a11 - a01 * a10;
-            q0 = a11 / det;
-            q1 = -a01 / det;
-            q2 = -a10 / det;
-            q3 = a00 / det;
-            const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
-            const bool ok = det != 0.0f && isfinite(det) && isfinite(q0) && isfinite(q1) && isfinite(q2) &&
-                            isfinite(q3) && r2 >= 0.0f;
-            if (ok) {
-                ex = sqrtf(r2 * (a00 * a00 + a01 * a01)) * 1.001f + 0.01f;
-                ey = sqrtf(r2 * (a10 * a10 + a11 * a11)) * 1.001f + 0.01f;
-            } else {
-                ex = -1.0f;
-                ey = -1.0f;
-            }
-        }
-        float4 *sp = reinterpret_cast<float4 *>(P.splats + i);
-        sp[0] = make_float4(cx, cy, ex, ey);
-        sp[1] = make_float4(q0, q1, q2, q3);
-        sp[2] = make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f,
-                            rgba[3]);
-    }
+    if (vis && P.splats) write_splat<FMT>(u, g, pr, P.splats + i);
 
     // ---- global offset: warp 0 looks back over the predecessors' published counts ----
     __syncthreads();
@@ -553,6 +595,112 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     }
 }
 
+// ---- several views of one model in one launch: the records are read once ------------------
+// Each CTA stages its 128 records once and runs the per-Gaussian work for every view of the
+// launch (each view with its own uniforms, outputs, control block and look-back flags).  Every
+// view's tile count is published right after that view's ballot; the look-backs run only after
+// all views are done, so predecessors have long published.  Per view the outputs are the ones
+// preprocess_kernel writes for that view alone.
+template <uint32_t FMT>
+__global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __grid_constant__ PreViewsParams P) {
+    constexpr uint32_t REC = (FMT == GS_FORMAT_FP32) ? 224u : 128u;
+    constexpr uint32_t C16 = REC / 16;
+    constexpr uint32_t ROW16 = (FMT == GS_FORMAT_FP32) ? C16 : C16 + 1;
+    constexpr uint32_t NW = kPreThreads / 32;
+    __shared__ __align__(16) uint4 s_rec[kPreThreads * ROW16];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ __align__(16) gs_frame_uniforms s_u;
+    __shared__ float s_key[kPreMaxViews][kPreThreads];
+    __shared__ uint32_t s_bal[kPreMaxViews][NW];
+    __shared__ uint32_t s_base[kPreMaxViews];
+    __shared__ uint32_t s_epoch[kPreMaxViews];
+    __shared__ uint32_t s_tile;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    const uint32_t nv = P.nviews;
+    if (tid == 0) {
+        s_tile = atomicAdd(&P.group->ticket[0], 1u);
+        if (FMT == GS_FORMAT_FP32) mbar_init(&s_bar, 1);
+    }
+    if (tid < nv) s_epoch[tid] = *(volatile uint32_t *)&P.views[tid].ctrl->epoch;
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t first = tile * kPreThreads;
+    const uint32_t cnt = min(kPreThreads, P.n - first);
+    stage_records<FMT>(s_rec, &s_bar, P.records, first, cnt, &P.group->status);
+
+    const uint32_t i = first + tid;
+    const bool sel = tid < cnt && gaussian_selected(P.selection, P.invert, i);
+    Rec g;
+    if (sel) g = load_rec<FMT>(s_rec + tid * ROW16);
+
+    for (uint32_t v = 0; v < nv; ++v) {
+        const PreView &V = P.views[v];
+        for (uint32_t k = tid; k < sizeof(gs_frame_uniforms) / 4; k += kPreThreads)
+            reinterpret_cast<uint32_t *>(&s_u)[k] = reinterpret_cast<const uint32_t *>(V.u)[k];
+        __syncthreads();
+        bool vis = false;
+        float key = 0.0f;
+        Proj pr;
+        if (sel) vis = gaussian_visible(s_u, g, pr, &key);
+        const uint32_t bal = __ballot_sync(0xFFFFFFFFu, vis);
+        if (lane == 0) s_bal[v][warp] = bal;
+        s_key[v][tid] = key;
+        if (vis && V.splats) write_splat<FMT>(s_u, g, pr, V.splats + i);
+        __syncthreads();  // s_bal[v] complete; s_u free for the next view
+        if (tid == 0) {
+            uint32_t total = 0;
+            for (uint32_t w = 0; w < NW; ++w) total += __popc(s_bal[v][w]);
+            s_base[v] = total;  // block total until the look-back
+            st_release(V.flags + tile, pack_flag(s_epoch[v], tile == 0 ? kFlagPrefix : kFlagAggregate, total));
+        }
+    }
+    __syncthreads();
+
+    // ---- global offsets: warp w looks back for views w, w + 4, ... ----
+    for (uint32_t v = warp; v < nv; v += NW) {
+        const PreView &V = P.views[v];
+        const uint32_t total = s_base[v];
+        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(V.flags, tile, s_epoch[v], &V.ctrl->status);
+        if (lane == 0) {
+            if (tile > 0) st_release(V.flags + tile, pack_flag(s_epoch[v], kFlagPrefix, prefix + total));
+            s_base[v] = prefix;
+            if (tile == P.ntiles - 1) {
+                const uint32_t c = prefix + total;
+                V.ctrl->count = c;
+                if (V.indirect) {
+                    V.indirect[0] = 6u;
+                    V.indirect[1] = c;
+                    V.indirect[2] = 0u;
+                    V.indirect[3] = 0u;
+                }
+                if (V.dispatch) {
+                    V.dispatch[0] = (c + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS;
+                    V.dispatch[1] = 1u;
+                    V.dispatch[2] = 1u;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t lt = lanemask_lt();
+    for (uint32_t v = 0; v < nv; ++v) {
+        const PreView &V = P.views[v];
+        if (tile == P.ntiles - 1) {
+            const uint32_t c = V.ctrl->count;
+            const uint32_t padded = min(((c + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS) * GS_SORT_BLOCK_KVS, V.depth_cap);
+            for (uint32_t k = c + tid; k < padded; k += kPreThreads) V.depths[k] = 2.0f;
+        }
+        const uint32_t bal = s_bal[v][warp];
+        if ((bal >> lane) & 1u) {
+            uint32_t off = s_base[v];
+            for (uint32_t w = 0; w < warp; ++w) off += __popc(s_bal[v][w]);
+            const uint32_t c = off + __popc(bal & lt);
+            V.indices[c] = i;
+            V.depths[c] = s_key[v][tid];
+        }
+    }
+}
+
 // `pre` + `post` for an empty model: zero counts, no padding beyond capacity.
 __global__ void preprocess_empty_kernel(uint32_t *indirect, uint32_t *dispatch, Ctrl *ctrl) {
     ctrl->count = 0;
@@ -567,6 +715,82 @@ __global__ void preprocess_empty_kernel(uint32_t *indirect, uint32_t *dispatch, 
         dispatch[1] = 1u;
         dispatch[2] = 1u;
     }
+}
+
+__global__ void ctrl_init_views_kernel(const PreView *views, uint32_t nviews, Ctrl *group) {
+    ctrl_reset(blockIdx.x < nviews ? views[blockIdx.x].ctrl : group, 1);
+}
+
+__global__ void preprocess_views_empty_kernel(const PreView *views, uint32_t nviews) {
+    for (uint32_t v = threadIdx.x; v < nviews; v += blockDim.x) {
+        const PreView &V = views[v];
+        V.ctrl->count = 0;
+        if (V.indirect) {
+            V.indirect[0] = 6u;
+            V.indirect[1] = 0u;
+            V.indirect[2] = 0u;
+            V.indirect[3] = 0u;
+        }
+        if (V.dispatch) {
+            V.dispatch[0] = 0u;
+            V.dispatch[1] = 1u;
+            V.dispatch[2] = 1u;
+        }
+    }
+}
+
+PreView preprocess_view(const gs_frame_uniforms *u_dev, uint32_t *indirect, uint32_t *dispatch, uint32_t *indices,
+                        float *depths, uint32_t depth_cap, gs_splat *splats, void *scratch) {
+    PreView V;
+    V.u = u_dev;
+    V.indirect = indirect;
+    V.dispatch = dispatch;
+    V.indices = indices;
+    V.depths = depths;
+    V.depth_cap = depth_cap;
+    V.splats = splats;
+    V.ctrl = reinterpret_cast<Ctrl *>(scratch);
+    V.flags = reinterpret_cast<uint64_t *>((uint8_t *)scratch + align_up(sizeof(Ctrl), 256));
+    return V;
+}
+
+cudaError_t launch_preprocess_views(const void *records, uint32_t format, uint32_t n, const uint32_t *selection,
+                                    int invert, const PreView *views, uint32_t nviews, void *group,
+                                    cudaStream_t st) {
+    if (nviews == 0) return cudaSuccess;
+    if (nviews > kPreMaxViews) return cudaErrorInvalidValue;
+    Ctrl *gctrl = reinterpret_cast<Ctrl *>(group);
+    ctrl_init_views_kernel<<<nviews + 1, 256, 0, st>>>(views, nviews, gctrl);
+    count_launches(1);
+    if (n == 0) {
+        preprocess_views_empty_kernel<<<1, 32, 0, st>>>(views, nviews);
+        count_launches(1);
+        return cudaGetLastError();
+    }
+    PreViewsParams P;
+    P.records = reinterpret_cast<const uint8_t *>(records);
+    P.n = n;
+    P.ntiles = (n + kPreThreads - 1) / kPreThreads;
+    P.selection = selection;
+    P.invert = invert ? 1u : 0u;
+    P.views = views;
+    P.nviews = nviews;
+    P.group = gctrl;
+    prof_mark(kProfPreprocess, true, st);
+    count_launches(1);
+    switch (format) {
+        case GS_FORMAT_FP32:
+            preprocess_views_kernel<GS_FORMAT_FP32><<<P.ntiles, kPreThreads, 0, st>>>(P);
+            break;
+        case GS_FORMAT_HALF_SH_FP16:
+            preprocess_views_kernel<GS_FORMAT_HALF_SH_FP16><<<P.ntiles, kPreThreads, 0, st>>>(P);
+            break;
+        default:
+            preprocess_views_kernel<GS_FORMAT_HALF_SH_BF16><<<P.ntiles, kPreThreads, 0, st>>>(P);
+            break;
+    }
+    prof_mark(kProfPreprocess, false, st);
+    return cudaGetLastError();
 }
 
 size_t preprocess_scratch_bytes(uint32_t n) {

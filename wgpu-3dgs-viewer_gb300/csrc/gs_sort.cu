@@ -22,26 +22,7 @@ constexpr uint32_t kTileKeys = kSortThreads * kSortRows;  // 3840
 constexpr uint32_t kSortWarps = kSortThreads / 32;
 static_assert(kTileKeys == GS_SORT_BLOCK_KVS, "block size must match the reference's");
 
-__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode) {
-    const uint32_t t = threadIdx.x;
-    if (t == 0) {
-        uint32_t e = ctrl->epoch + 1u;
-        if (e >= (1u << 30) || e == 0u) e = 1u;
-        ctrl->epoch = e;
-        ctrl->ticket[0] = 0u;
-        ctrl->ticket[1] = 0u;
-        if (mode == 1) {
-            ctrl->status = 0u;
-            for (int k = 1; k < 8; ++k) ctrl->ticket[k] = 0u;
-            ctrl->count = 0u;
-            ctrl->total = 0u;
-            ctrl->pair_base = 0u;
-            ctrl->seg_total = 0u;
-        }
-    }
-    if (mode == 1)
-        for (uint32_t k = t; k < 4 * 256; k += blockDim.x) (&ctrl->hist[0][0])[k] = 0u;
-}
+__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode) { ctrl_reset(ctrl, mode); }
 
 __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t max_count) {
     return count ? min(*count, max_count) : max_count;
