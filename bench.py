@@ -160,8 +160,9 @@ def cpu_baseline(args, scene, pods, threads):
 
 def measure_tiers(args, scene, pods, stream, plain_fps):
     """The tiers built on the plain path, on the same workload: multi-view batches (one CUDA graph
-    per batch shape), compressed records (FP16 rotation/scale, BF16 SH), and serving (open-loop
-    Poisson arrivals at 80% of the measured peak request rate, p50/p99 latency)."""
+    per batch shape, records read once per model, launch choices from the autotuner), compressed
+    records (FP16 rotation/scale, BF16 SH), and serving (open-loop Poisson arrivals at 80% of the
+    measured peak request rate, p50/p99 latency)."""
     import torch
 
     import gs300
@@ -176,9 +177,14 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
         batch = gs300.Batch(mv, [key])
         targets = [gs300.RenderTarget(W, H) for _ in range(B)]
 
-        def go(r):
-            batch.render([(key, pods[(r * B + i) % 120], targets[i]) for i in range(B)], stream=sh)
+        def views(r):
+            return [(key, pods[(r * B + i) % 120], targets[i]) for i in range(B)]
 
+        def go(r):
+            batch.render(views(r), stream=sh)
+
+        # launch choices picked by the autotuner on this batch shape (frames are the same for all)
+        tuning, _ = batch.autotune(views(0), reps=2)
         go(0)
         batch.synchronize(stream=sh)
         for r in range(2):
@@ -193,7 +199,7 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
         batch.synchronize(stream=sh)
         fps = B * reps / (e0.elapsed_time(e1) / 1000.0)
         batch.close()
-        return fps
+        return fps, tuning
 
     def plain_fps_of(viewer, reps):
         t = gs300.RenderTarget(W, H)
@@ -213,7 +219,7 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
     reps = max(2, args.steps // B)
     mv32 = gs300.MultiModelViewer()
     mv32.insert_model("scene", scene)
-    out["batched_fp32_fps"] = batch_fps(mv32, "scene", reps)
+    out["batched_fp32_fps"], out["batched_fp32_tuning"] = batch_fps(mv32, "scene", reps)
     out["batch_views"] = B
     mv32.close()
 
@@ -223,7 +229,7 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
     v16.close()
     mv16 = gs300.MultiModelViewer()
     mv16.insert_model("scene", half, fmt=R.FORMAT_HALF_SH_BF16)
-    out["batched_fp16_fps"] = batch_fps(mv16, "scene", reps)
+    out["batched_fp16_fps"], out["batched_fp16_tuning"] = batch_fps(mv16, "scene", reps)
 
     # serving: closed loop to find the peak request rate, then Poisson arrivals at 80% of it
     need = gs300.Server.request_bytes(args.n, W, H)

@@ -341,6 +341,27 @@ gs_status gs_batch_render(gs_batch *batch, const gs_batch_view *views, uint32_t 
 /* Wait, check every view's device status, regrow overflowed tile-pair lists and re-render. */
 gs_status gs_batch_synchronize(gs_batch *batch, gs_stream stream);
 
+/* Launch choices of a batch that change its speed, never its frames. */
+typedef struct gs_tuning {
+    uint32_t suffix_min;       /* raster: tile lists at least this long take the exact early-out (>= 1) */
+    float eps;                 /* raster: transmittance ending the front-to-back walk, (0, 0.5] */
+    uint32_t views_per_launch; /* views of one model sharing a preprocess launch, 1..16 */
+    uint32_t streams;          /* streams the captured graph fans out over, 1..16 */
+    uint32_t sort_match;       /* depth sort ranking: 1 = match.any, 0 = one ballot per digit bit */
+    uint32_t hist_blocks;      /* depth sort key-histogram blocks, 0 (by key count) or 1..1216 */
+} gs_tuning;
+/* The library's defaults (GS300_SUFFIX_MIN / GS300_SUFFIX_EPS override the raster knobs). */
+gs_status gs_tuning_default(gs_tuning *out);
+/* GS_ERR_INVALID_ARG outside the ranges above.  The next render re-captures the graph. */
+gs_status gs_batch_set_tuning(gs_batch *batch, const gs_tuning *tuning);
+gs_status gs_batch_get_tuning(gs_batch *batch, gs_tuning *out);
+/* Autotuner: renders `views` (into their targets) under candidate tunings, one knob at a time
+ * (coordinate descent from the current tuning, `rounds` sweeps), timing `reps` renders of each
+ * with CUDA events after one warm-up, and keeps the fastest.  The chosen tuning is set on the
+ * batch and returned with its milliseconds per batch.  Synchronous. */
+gs_status gs_batch_autotune(gs_batch *batch, const gs_batch_view *views, uint32_t view_count, uint32_t reps,
+                            uint32_t rounds, gs_tuning *out_best, double *out_ms);
+
 /* ------------------------------------------------------------------------------------------ */
 /* Serving (no counterpart in the reference): scenes stay resident (the models of a           */
 /* MultiModelViewer); (scene, camera, resolution) requests are admitted first come first      */

@@ -134,3 +134,9 @@ def test_scratch_sizes_grow_with_problem(gs):
     assert L.gs_rasterize_scratch_bytes(1000, 1920, 1080, 8000) > L.gs_rasterize_scratch_bytes(1000, 64, 64, 8000)
     # keys_buffer_size(n) of the reference (src/radix_sorter.rs:931-934): rounded up to 3840
     assert L.gs_depth_capacity(1) == 3840 and L.gs_depth_capacity(3840) == 3840 and L.gs_depth_capacity(3841) == 7680
+
+
+def test_tuning_default(gs):
+    t = gs.tuning_default()
+    assert t == {"suffix_min": 1536, "eps": pytest.approx(1e-6), "views_per_launch": 16, "streams": 16,
+                 "sort_match": 1, "hist_blocks": 0}

@@ -91,3 +91,61 @@ def test_batch_shared_record_reads(gs, cuda, monkeypatch):
                 assert (got[..., :3] == 0).all() and (got[..., 3] == 255).all()
                 continue
             assert np.array_equal(got, _single(gs, sc, mt, cam, w, h, fmt))
+
+
+TUNINGS = [
+    dict(views_per_launch=1, streams=1),
+    dict(suffix_min=1, eps=0.3),            # every tile takes the early-out, with frequent restarts
+    dict(sort_match=0, hist_blocks=7, views_per_launch=3, streams=5),
+]
+
+
+@pytest.mark.parametrize("knobs", TUNINGS, ids=["serial", "early_out_everywhere", "ballot_sort"])
+def test_batch_tuning_changes_no_frame(gs, cuda, monkeypatch, knobs):
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(40_000, seed=12)
+    mv = gs.MultiModelViewer()
+    mv.insert_model("m", sc)
+    batch = gs.Batch(mv, ["m"])
+    batch.set_tuning(**knobs)
+    assert all(batch.tuning[k] == pytest.approx(v) for k, v in knobs.items())
+    plan = [(320, 180), (256, 256), (640, 360), (200, 120), (320, 180)]
+    targets = [gs.RenderTarget(w, h) for w, h in plan]
+    cams = [S.orbit_camera(9 * j + 2, radius=5.5) for j in range(len(plan))]
+    batch.render([("m", gs.CameraPod.new(c, wh), t) for wh, c, t in zip(plan, cams, targets)])
+    batch.synchronize()
+    mt = gs.model_transform_pod()
+    for (w, h), cam, t in zip(plan, cams, targets):
+        assert np.array_equal(t.download(), _single(gs, sc, mt, cam, w, h))
+
+
+def test_batch_tuning_rejects_bad_values(gs, cuda):
+    mv = gs.MultiModelViewer()
+    mv.insert_model("m", S.synth_scene(100, seed=1))
+    batch = gs.Batch(mv, ["m"])
+    for bad in (dict(views_per_launch=0), dict(views_per_launch=17), dict(streams=0), dict(streams=17),
+                dict(sort_match=2), dict(eps=0.0), dict(eps=0.7), dict(suffix_min=0), dict(hist_blocks=5000)):
+        with pytest.raises(gs.GsError):
+            batch.set_tuning(**bad)
+    assert batch.tuning == gs.tuning_default()
+
+
+def test_batch_autotune(gs, cuda, monkeypatch):
+    """The autotuner returns a valid tuning, leaves it set, and the frames stay the single-view ones."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(60_000, seed=13)
+    mv = gs.MultiModelViewer()
+    mv.insert_model("m", sc)
+    batch = gs.Batch(mv, ["m"])
+    plan = [(480, 270)] * 4
+    targets = [gs.RenderTarget(w, h) for w, h in plan]
+    cams = [S.orbit_camera(30 * j, radius=6.0) for j in range(len(plan))]
+    views = [("m", gs.CameraPod.new(c, wh), t) for wh, c, t in zip(plan, cams, targets)]
+    best, ms = batch.autotune(views, reps=2)
+    assert ms > 0 and batch.tuning == best
+    assert 1 <= best["views_per_launch"] <= 16 and 1 <= best["streams"] <= 16
+    batch.render(views)
+    batch.synchronize()
+    mt = gs.model_transform_pod()
+    for (w, h), cam, t in zip(plan, cams, targets):
+        assert np.array_equal(t.download(), _single(gs, sc, mt, cam, w, h))

@@ -1062,6 +1062,7 @@ struct gs_batch {
     DevBuf views_dev;                       // PreView per view (device), rebuilt with the graph
     DevBuf group_dev;                       // one control block per multi-view launch
     uint32_t chunks = 0;
+    gs::Tuning tuning = gs::default_tuning();
     cudaStream_t capture = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::string shape;
@@ -1129,9 +1130,10 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
             GS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             b->events.push_back(e);
         }
-        const uint32_t nstreams = n < kBatchStreams ? n : kBatchStreams;
+        const uint32_t nstreams = std::min(n, std::min(b->tuning.streams, kBatchStreams));
+        const size_t per_launch = std::min(b->tuning.views_per_launch, kPreMaxViews);
         // Views of one model share its record reads: one preprocess launch per chunk of up to
-        // kPreMaxViews views of the same model, in order of first appearance.
+        // `per_launch` views of the same model, in order of first appearance.
         std::vector<std::vector<uint32_t>> chunks;
         {
             std::vector<const Model *> seen;
@@ -1146,8 +1148,8 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
                 by_model[g].push_back(i);
             }
             for (auto &grp : by_model)
-                for (size_t k = 0; k < grp.size(); k += kPreMaxViews)
-                    chunks.emplace_back(grp.begin() + k, grp.begin() + std::min(grp.size(), k + kPreMaxViews));
+                for (size_t k = 0; k < grp.size(); k += per_launch)
+                    chunks.emplace_back(grp.begin() + k, grp.begin() + std::min(grp.size(), k + per_launch));
         }
         const gs_frame_uniforms *udev = reinterpret_cast<const gs_frame_uniforms *>(b->uniforms_dev.ptr);
         std::vector<PreView> pv(n);
@@ -1199,13 +1201,13 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
                 if (vs != cs) err = cudaStreamWaitEvent(vs, b->chunk_events[c], 0);
                 if (err == cudaSuccess)
                     err = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, ms[i]->n, ind + 1, 32,
-                                      v.sort_scratch.ptr, vs);
+                                      v.sort_scratch.ptr, vs, kProfDepthSort, &b->tuning);
                 if (err == cudaSuccess) {
                     const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1,
                                             ms[i]->n};
                     err = launch_raster(&seg, 1, b->uniforms_host[i], views[i].target, views[i].width,
                                         views[i].height, views[i].pitch, v.max_pairs, v.raster_scratch.ptr,
-                                        mv->frame.exact_exp, vs);
+                                        mv->frame.exact_exp, vs, &b->tuning);
                 }
             }
         }
@@ -1297,6 +1299,165 @@ gs_status gs_batch_synchronize(gs_batch *b, gs_stream stream) {
         if (s != GS_OK) return s;
     }
     return fail(GS_ERR_CAPACITY, "tile-pair list kept overflowing");
+}
+
+}  // extern "C"
+
+namespace {
+
+gs_tuning to_public(const gs::Tuning &t) {
+    gs_tuning o;
+    o.suffix_min = t.suffix_min;
+    o.eps = t.eps;
+    o.views_per_launch = t.views_per_launch;
+    o.streams = t.streams;
+    o.sort_match = t.sort_match;
+    o.hist_blocks = t.hist_blocks;
+    return o;
+}
+
+gs_status from_public(const gs_tuning *p, gs::Tuning *t) {
+    if (!p) return fail(GS_ERR_INVALID_ARG, "tuning is NULL");
+    if (p->suffix_min < 1) return fail(GS_ERR_INVALID_ARG, "suffix_min must be >= 1");
+    if (!(p->eps > 0.0f && p->eps <= 0.5f)) return fail(GS_ERR_INVALID_ARG, "eps %g outside (0, 0.5]", (double)p->eps);
+    if (p->views_per_launch < 1 || p->views_per_launch > kPreMaxViews)
+        return fail(GS_ERR_INVALID_ARG, "views_per_launch %u outside 1..%u", p->views_per_launch, kPreMaxViews);
+    if (p->streams < 1 || p->streams > kBatchStreams)
+        return fail(GS_ERR_INVALID_ARG, "streams %u outside 1..%u", p->streams, kBatchStreams);
+    if (p->sort_match > 1) return fail(GS_ERR_INVALID_ARG, "sort_match must be 0 or 1");
+    if (p->hist_blocks > 152 * 8) return fail(GS_ERR_INVALID_ARG, "hist_blocks %u above 1216", p->hist_blocks);
+    t->suffix_min = p->suffix_min;
+    t->eps = p->eps;
+    t->views_per_launch = p->views_per_launch;
+    t->streams = p->streams;
+    t->sort_match = p->sort_match;
+    t->hist_blocks = p->hist_blocks;
+    return GS_OK;
+}
+
+void set_tuning_locked(gs_batch *b, const gs::Tuning &t) {
+    b->tuning = t;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;  // the next render captures the graph again
+}
+
+}  // namespace
+
+extern "C" {
+
+gs_status gs_tuning_default(gs_tuning *out) {
+    if (!out) return fail(GS_ERR_INVALID_ARG, "out is NULL");
+    *out = to_public(gs::default_tuning());
+    return GS_OK;
+}
+
+gs_status gs_batch_set_tuning(gs_batch *b, const gs_tuning *tuning) {
+    if (!b) return fail(GS_ERR_INVALID_ARG, "batch is NULL");
+    gs::Tuning t;
+    const gs_status s = from_public(tuning, &t);
+    if (s != GS_OK) return s;
+    std::lock_guard<std::mutex> g(b->mu);
+    set_tuning_locked(b, t);
+    return GS_OK;
+}
+
+gs_status gs_batch_get_tuning(gs_batch *b, gs_tuning *out) {
+    if (!b || !out) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> g(b->mu);
+    *out = to_public(b->tuning);
+    return GS_OK;
+}
+
+gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n, uint32_t reps, uint32_t rounds,
+                            gs_tuning *out_best, double *out_ms) {
+    if (!b || (n && !views)) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    if (n == 0) return fail(GS_ERR_INVALID_ARG, "autotune needs at least one view");
+    if (reps == 0) reps = 1;
+    if (rounds == 0) rounds = 1;
+    std::lock_guard<std::mutex> g(b->mu);
+    cudaStream_t st = nullptr;
+    GS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    GS_CUDA(cudaEventCreate(&e0));
+    GS_CUDA(cudaEventCreate(&e1));
+    // Milliseconds per batch under tuning t (one warm-up render, which also captures the graph
+    // and grows any tile-pair list that overflowed, then `reps` timed renders).
+    auto measure = [&](const gs::Tuning &t, double *ms) -> gs_status {
+        set_tuning_locked(b, t);
+        for (int attempt = 0; attempt < 4; ++attempt) {
+            gs_status s = batch_render_locked(b, views, n, st);
+            if (s != GS_OK) return s;
+            GS_CUDA(cudaStreamSynchronize(st));
+            bool regrow = false;
+            for (uint32_t i = 0; i < n; ++i) {
+                Ctrl c{};
+                GS_CUDA(cudaMemcpy(&c, b->slots[i].raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+                if (c.status & kStatusTimeout) return status_from_bits(c.status, "autotune");
+                if (c.status & kStatusCapacity) {
+                    uint64_t p = (uint64_t)c.total + c.total / 4 + 4096;
+                    b->slots[i].max_pairs = p > 0x7FFFFFFFull ? 0x7FFFFFFFu : (uint32_t)p;
+                    b->slots[i].raster_scratch.release();
+                    regrow = true;
+                }
+            }
+            if (!regrow) break;
+        }
+        GS_CUDA(cudaEventRecord(e0, st));
+        for (uint32_t r = 0; r < reps; ++r) {
+            const gs_status s = batch_render_locked(b, views, n, st);
+            if (s != GS_OK) return s;
+        }
+        GS_CUDA(cudaEventRecord(e1, st));
+        GS_CUDA(cudaEventSynchronize(e1));
+        float f = 0.0f;
+        GS_CUDA(cudaEventElapsedTime(&f, e0, e1));
+        *ms = (double)f / reps;
+        return GS_OK;
+    };
+    gs::Tuning best = b->tuning;
+    double best_ms = 0.0;
+    gs_status s = measure(best, &best_ms);
+    // Candidate values per knob; every combination renders the same frames.
+    const uint32_t suffix_c[] = {1024, 1536, 2048, 3072};
+    const float eps_c[] = {1e-6f, 1e-5f};
+    const uint32_t vpl_c[] = {1, 4, 8, 16};
+    const uint32_t streams_c[] = {4, 8, 16};
+    const uint32_t match_c[] = {0, 1};
+    const uint32_t hist_c[] = {0, 304, 608};
+    for (uint32_t round = 0; round < rounds && s == GS_OK; ++round) {
+        for (int knob = 0; knob < 6 && s == GS_OK; ++knob) {
+            const size_t nc = knob == 0 ? 4 : knob == 1 ? 2 : knob == 2 ? 4 : knob == 3 ? 3 : knob == 4 ? 2 : 3;
+            for (size_t c = 0; c < nc && s == GS_OK; ++c) {
+                gs::Tuning t = best;
+                switch (knob) {
+                    case 0: t.suffix_min = suffix_c[c]; break;
+                    case 1: t.eps = eps_c[c]; break;
+                    case 2: t.views_per_launch = vpl_c[c]; break;
+                    case 3: t.streams = streams_c[c]; break;
+                    case 4: t.sort_match = match_c[c]; break;
+                    default: t.hist_blocks = hist_c[c]; break;
+                }
+                if (t.suffix_min == best.suffix_min && t.eps == best.eps && t.views_per_launch == best.views_per_launch &&
+                    t.streams == best.streams && t.sort_match == best.sort_match && t.hist_blocks == best.hist_blocks)
+                    continue;
+                double ms = 0.0;
+                s = measure(t, &ms);
+                if (s == GS_OK && ms < best_ms) {
+                    best_ms = ms;
+                    best = t;
+                }
+            }
+        }
+    }
+    set_tuning_locked(b, best);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (s != GS_OK) return s;
+    if (out_best) *out_best = to_public(best);
+    if (out_ms) *out_ms = best_ms;
+    return GS_OK;
 }
 
 }  // extern "C"

@@ -63,10 +63,24 @@ gs_status ply_check_layout(const gs_ply_layout *layout);
 cudaError_t launch_ply_convert(const void *vertices, const gs_ply_layout &layout, uint32_t format, void *records,
                                cudaStream_t st);
 
+// Launch choices that change speed, never results (gs_tuning in the C ABI).  The defaults are
+// the library's; batches can set them or have them picked by gs_batch_autotune.
+struct Tuning {
+    uint32_t suffix_min = 1536;     // raster: tile lists at least this long take the exact early-out
+    float eps = 1e-6f;              // raster: transmittance that ends the front-to-back walk
+    uint32_t views_per_launch = 16; // batch: views per shared-read preprocess launch (1..16)
+    uint32_t streams = 16;          // batch: streams the captured graph fans out over (1..16)
+    uint32_t sort_match = 1;        // depth sort: 1 = match.any ranking, 0 = a ballot per digit bit
+    uint32_t hist_blocks = 0;       // depth sort: key-histogram grid (0 = by key count, <= 1216)
+};
+// The defaults, with GS300_SUFFIX_MIN / GS300_SUFFIX_EPS overriding the raster knobs.
+Tuning default_tuning();
+
 // ---- K2 onesweep radix sort (gs_sort.cu) ----
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits);
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
-                        uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage = kProfDepthSort);
+                        uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage = kProfDepthSort,
+                        const Tuning *tuning = nullptr);
 
 // Packed (uint2 {key, value}) in-place sort for internal pair lists whose digit histograms
 // the producer accumulated into the control block after sort_pairs_begin().
@@ -87,7 +101,8 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t width, uint32_t height
 // exact_exp: 1 = the portable exp (bit-identical with the CPU oracle), 0 = the SFU exp.
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u,
                           uint8_t *target, uint32_t width, uint32_t height, uint32_t pitch,
-                          uint32_t max_pairs, void *scratch, int exact_exp, cudaStream_t st);
+                          uint32_t max_pairs, void *scratch, int exact_exp, cudaStream_t st,
+                          const Tuning *tuning = nullptr);
 // Scratch control block of a raster call (status, pair counts).
 const Ctrl *raster_ctrl(const void *scratch);
 

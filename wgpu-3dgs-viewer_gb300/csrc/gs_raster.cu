@@ -86,19 +86,11 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_
 
 const Ctrl *raster_ctrl(const void *scratch) { return reinterpret_cast<const Ctrl *>(scratch); }
 
-// Early-out knobs of the rasteriser (results are identical for any values): tiles with fewer
-// list entries than `suffix_min` take the single pass; `eps` is the transmittance that ends the
-// front-to-back walk.  Overridable for tuning by GS300_SUFFIX_MIN / GS300_SUFFIX_EPS.
-struct RasterTuning {
-    uint32_t suffix_min;
-    float eps;
-};
-
-static RasterTuning raster_tuning() {
-    RasterTuning r{1536u, 1e-6f};
-    if (const char *v = getenv("GS300_SUFFIX_MIN")) r.suffix_min = (uint32_t)strtoul(v, nullptr, 10);
-    if (const char *v = getenv("GS300_SUFFIX_EPS")) r.eps = strtof(v, nullptr);
-    return r;
+Tuning default_tuning() {
+    Tuning t;
+    if (const char *v = getenv("GS300_SUFFIX_MIN")) t.suffix_min = (uint32_t)strtoul(v, nullptr, 10);
+    if (const char *v = getenv("GS300_SUFFIX_EPS")) t.eps = strtof(v, nullptr);
+    return t;
 }
 
 // Tile rectangle of a splat's fragment box; false when it touches no tile.
@@ -677,8 +669,7 @@ cudaError_t raster_counters(unsigned long long out[4], bool reset) {
 template <uint32_t MODE>
 static void launch_raster_mode(const RasterLayout &L, const gs_splat *splats, uint8_t *target, uint32_t W, uint32_t H,
                                uint32_t pitch, float std2, float outline2, int exact, uint32_t max_splats,
-                               cudaStream_t st) {
-    const RasterTuning t = raster_tuning();
+                               cudaStream_t st, const Tuning &t) {
     if (exact) {
         raster_kernel<MODE, true, false><<<L.ntiles, kRasterThreads, 0, st>>>(
             splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
@@ -698,7 +689,8 @@ static void launch_raster_mode(const RasterLayout &L, const gs_splat *splats, ui
 
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
                           uint32_t W, uint32_t H, uint32_t pitch, uint32_t max_pairs, void *scratch, int exact_exp,
-                          cudaStream_t st) {
+                          cudaStream_t st, const Tuning *tuning) {
+    const Tuning tn = tuning ? *tuning : default_tuning();
     uint32_t max_splats = 0;
     for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
     const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
@@ -757,13 +749,13 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     count_launches(1);
     switch (u.display_mode) {
         case GS_DISPLAY_SPLAT:
-            launch_raster_mode<GS_DISPLAY_SPLAT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st);
+            launch_raster_mode<GS_DISPLAY_SPLAT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st, tn);
             break;
         case GS_DISPLAY_ELLIPSE:
-            launch_raster_mode<GS_DISPLAY_ELLIPSE>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st);
+            launch_raster_mode<GS_DISPLAY_ELLIPSE>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st, tn);
             break;
         default:
-            launch_raster_mode<GS_DISPLAY_POINT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st);
+            launch_raster_mode<GS_DISPLAY_POINT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st, tn);
             break;
     }
     prof_mark(kProfRaster, false, st);

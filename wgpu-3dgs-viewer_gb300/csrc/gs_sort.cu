@@ -348,8 +348,38 @@ static uint32_t grid_for(uint32_t max_count) {
     return blocks ? blocks : 1;
 }
 
+template <bool MATCH>
+static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
+                               uint32_t key_bits, const SortLayout &L, cudaStream_t st) {
+    const uint32_t npasses = sort_passes(key_bits);
+    const size_t fstride = (size_t)L.ntiles * 256;
+    if (npasses == 1) {
+        sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
+        unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
+        count_launches(2);
+        return;
+    }
+    uint2 *src = L.alt_a, *dst = L.alt_b;
+    sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
+    for (uint32_t p = 1; p + 1 < npasses; ++p) {
+        sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, pass_bits(key_bits, p), L.ctrl,
+            L.flags + p * fstride);
+        uint2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, pass_bits(key_bits, npasses - 1),
+        L.ctrl, L.flags + (npasses - 1) * fstride);
+    count_launches(npasses);
+}
+
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
-                        uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage) {
+                        uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage, const Tuning *tuning) {
+    const Tuning tn = tuning ? *tuning : Tuning{};
     const uint32_t npasses = sort_passes(key_bits);
     const SortLayout L = sort_layout(scratch, max_count, npasses);
     ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1);
@@ -358,33 +388,13 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     prof_mark(prof_stage, true, st);
     uint32_t hist_blocks = (max_count + 256 * 4 * 4 - 1) / (256 * 4 * 4);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
+    if (tn.hist_blocks) hist_blocks = tn.hist_blocks < 152 * 8 ? tn.hist_blocks : 152 * 8;
     sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, key_bits, L.ctrl);
     count_launches(1);
-    const size_t fstride = (size_t)L.ntiles * 256;
-    if (npasses == 1) {
-        sort_pass_kernel<false, true, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, L.alt_a,
-                                                                        count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
-        unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
-        count_launches(2);
-    } else {
-        uint2 *src = L.alt_a, *dst = L.alt_b;
-        sort_pass_kernel<false, true, true><<<L.ntiles, kSortThreads, 0, st>>>(keys, vals, nullptr, nullptr, nullptr, src,
-                                                                        count, max_count, 0, pass_bits(key_bits, 0),
-                                                                        L.ctrl, L.flags);
-        for (uint32_t p = 1; p + 1 < npasses; ++p) {
-            sort_pass_kernel<true, true, true><<<L.ntiles, kSortThreads, 0, st>>>(
-                nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, pass_bits(key_bits, p), L.ctrl,
-                L.flags + p * fstride);
-            uint2 *t = src;
-            src = dst;
-            dst = t;
-        }
-        sort_pass_kernel<true, false, true><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, keys, vals, nullptr, count,
-                                                                        max_count, npasses - 1,
-                                                                        pass_bits(key_bits, npasses - 1), L.ctrl,
-                                                                        L.flags + (npasses - 1) * fstride);
-        count_launches(npasses);
-    }
+    if (tn.sort_match)
+        launch_sort_passes<true>(keys, vals, max_count, count, key_bits, L, st);
+    else
+        launch_sort_passes<false>(keys, vals, max_count, count, key_bits, L, st);
     prof_mark(prof_stage, false, st);
     return cudaGetLastError();
 }

@@ -174,6 +174,13 @@ def _file_bytes(path_or_bytes):
         return f.read()
 
 
+def tuning_default():
+    """gs_tuning_default: the library's launch choices for batches."""
+    t = records.Tuning()
+    check(lib().gs_tuning_default(ctypes.byref(t)))
+    return t.as_dict()
+
+
 def ply_parse_header(path_or_bytes):
     """gs_ply_parse_header: the PlyLayout (field offsets, count, stride) of a PLY file."""
     data = _file_bytes(path_or_bytes)
@@ -386,8 +393,7 @@ class Batch:
         check(lib().gs_batch_create(viewer._h, arr, len(self.keys), ctypes.byref(h)))
         self._h = h
 
-    def render(self, views, stream=None):
-        """views: iterable of (key or model index, CameraPod, target)."""
+    def _views(self, views):
         views = list(views)
         arr = (records.BatchView * max(1, len(views)))()
         for i, (model, pod, target) in enumerate(views):
@@ -396,7 +402,39 @@ class Batch:
             arr[i].model, arr[i].width, arr[i].height, arr[i].pitch = idx, w, h, pitch
             arr[i].target = ptr
             arr[i].camera = pod
-        check(lib().gs_batch_render(self._h, ctypes.cast(arr, ctypes.c_void_p), len(views), _stream(stream)))
+        return arr, len(views)
+
+    def render(self, views, stream=None):
+        """views: iterable of (key or model index, CameraPod, target)."""
+        arr, n = self._views(views)
+        check(lib().gs_batch_render(self._h, ctypes.cast(arr, ctypes.c_void_p), n, _stream(stream)))
+
+    @property
+    def tuning(self):
+        t = records.Tuning()
+        check(lib().gs_batch_get_tuning(self._h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **knobs):
+        """Change launch choices (suffix_min, eps, views_per_launch, streams, sort_match,
+        hist_blocks); frames stay the same."""
+        t = records.Tuning()
+        check(lib().gs_batch_get_tuning(self._h, ctypes.byref(t)))
+        for k, v in knobs.items():
+            if k not in t.as_dict():
+                raise GsError(1, f"unknown tuning knob {k}")
+            setattr(t, k, v)
+        check(lib().gs_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self, views, reps=3, rounds=1):
+        """gs_batch_autotune: times these views under candidate tunings and keeps the fastest.
+        Returns (tuning dict, ms per batch)."""
+        arr, n = self._views(views)
+        t = records.Tuning()
+        ms = ctypes.c_double()
+        check(lib().gs_batch_autotune(self._h, ctypes.cast(arr, ctypes.c_void_p), n, int(reps), int(rounds),
+                                      ctypes.byref(t), ctypes.byref(ms)))
+        return t.as_dict(), ms.value
 
     def synchronize(self, stream=None):
         check(lib().gs_batch_synchronize(self._h, _stream(stream)))

@@ -102,6 +102,10 @@ SIGNATURES = [
     ("gs_batch_destroy", None, [P]),
     ("gs_batch_render", ST, [P, P, U32, P]),
     ("gs_batch_synchronize", ST, [P, P]),
+    ("gs_tuning_default", ST, [P]),
+    ("gs_batch_set_tuning", ST, [P, P]),
+    ("gs_batch_get_tuning", ST, [P, P]),
+    ("gs_batch_autotune", ST, [P, P, U32, U32, U32, P, P]),
     ("gs_server_create", ST, [P, SZ, U32, PP]),
     ("gs_server_destroy", None, [P]),
     ("gs_server_request_bytes", SZ, [U32, U32, U32]),

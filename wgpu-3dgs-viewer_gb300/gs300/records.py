@@ -175,6 +175,22 @@ class BatchView(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    """gs_tuning: launch choices of a batch that change its speed, never its frames."""
+
+    _fields_ = [
+        ("suffix_min", ctypes.c_uint32),
+        ("eps", ctypes.c_float),
+        ("views_per_launch", ctypes.c_uint32),
+        ("streams", ctypes.c_uint32),
+        ("sort_match", ctypes.c_uint32),
+        ("hist_blocks", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class ServerReport(ctypes.Structure):
     """gs_server_report: request counts and submit-to-completion latency percentiles."""
 
