@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--no-tiers", action="store_true")
     ap.add_argument("--batch-views", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=4)
+    ap.add_argument("--precision", action="store_true",
+                    help="precision report instead of the benchmark: FP32 and half records against "
+                    "the host FP64 oracle over --precision-cameras orbit cameras")
+    ap.add_argument("--precision-cameras", type=int, default=32)
     return ap.parse_args()
 
 
@@ -340,8 +344,54 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_precision(args):
+    """Per-frame error of the GPU path against the host FP64 oracle of the same pipeline (same
+    pods, same records): FP32 records, then FP16 rotation/scale with FP16 SH and with BF16 SH.
+    Prints one JSON line; the oracle runs on all host cores."""
+    import torch
+
+    import gs300
+    from gs300 import records as R
+    from gs300 import scene as S
+    from oracle import oracle as O
+
+    W, H, K = args.width, args.height, args.precision_cameras
+    threads = os.cpu_count() or 1
+    cams = [S.orbit_camera(int(k * 120 / K)) for k in range(K)]
+    out = {"metric": "precision vs FP64 oracle", "config": dict(workload(args), cameras=K), "oracle_threads": threads}
+    for name, fmt in (("fp32", R.FORMAT_FP32), ("half_sh_fp16", R.FORMAT_HALF_SH_FP16),
+                      ("half_sh_bf16", R.FORMAT_HALF_SH_BF16)):
+        sc = S.synth_scene(args.n, seed=args.seed, fmt=fmt)
+        v = gs300.Viewer(sc, fmt=None if fmt == R.FORMAT_FP32 else fmt)
+        t = gs300.RenderTarget(W, H)
+        psnr, maxerr, within1 = [], [], []
+        t0 = time.perf_counter()
+        for cam in cams:
+            pod = gs300.CameraPod.new(cam, (W, H))
+            v.update_camera_with_pod(pod)
+            v.render(t)
+            v.synchronize()
+            got = t.download()
+            ref, _ = O.render64(pod, gs300.model_transform_pod(), gs300.gaussian_transform_pod(), sc, fmt, W, H,
+                                threads=threads)
+            d = got[..., :3].astype(np.int32) - ref[..., :3].astype(np.int32)
+            mse = float((d.astype(np.float64) ** 2).mean())
+            psnr.append(math.inf if mse == 0 else 10.0 * math.log10(255.0 ** 2 / mse))
+            maxerr.append(int(np.abs(d).max()))
+            within1.append(float((np.abs(d).max(axis=-1) <= 1).mean()))
+        out[name] = {"psnr_db_min": min(psnr), "psnr_db_mean": statistics.mean(psnr), "max_err_max": max(maxerr),
+                     "max_err_per_frame": maxerr, "within_1_min": min(within1),
+                     "psnr_db_per_frame": [round(p, 2) for p in psnr], "seconds": time.perf_counter() - t0}
+        v.close()
+        torch.cuda.synchronize()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.precision:
+        run_precision(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
