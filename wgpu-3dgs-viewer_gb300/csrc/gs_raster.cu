@@ -420,7 +420,7 @@ __device__ __forceinline__ bool fragment(const float4 a, const float4 b, float p
 }
 
 // BlendState::ALPHA_BLENDING onto an 8-bit channel, in units of 1/255: round(d·(1-α) + s·α).
-__device__ __forceinline__ float blend8(float d, float om, float s_alpha) { return rint_small(fmaf(d, om, s_alpha)); }
+__device__ __forceinline__ float blend8(float d, float om, float s_alpha) { return rintf(fmaf(d, om, s_alpha)); }
 
 struct RasterShared {
     float4 a[kRasterThreads];    // cx, cy, r² limit, alpha
