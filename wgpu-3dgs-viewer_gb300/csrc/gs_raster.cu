@@ -291,53 +291,70 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
     }
 }
 
-// K3c: emission of the (tile, value) pairs of 256 draw ranks, load-balanced over the CTA, plus
-// the digit histograms of the tile ids for the tile sort.
+// K3c: every splat writes its (tile, value) pairs at its scanned offset, its kept tiles in
+// row-major order.  A thread walks its own tile rectangle; a splat with more than kWarpEmit
+// tiles is written by its whole warp, 32 pairs at a time, so one large splat does not hold up
+// the others.  Also accumulates the tile-key digit histograms of the tile sort: each CTA loops
+// over chunks of 256 ranks (grid-stride) and adds its shared histograms to the global ones once,
+// which keeps the global atomics on those few hundred bins to a few per CTA.
+constexpr uint32_t kWarpEmit = 32;
+
 __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
     const uint4 *__restrict__ info, const uint32_t *__restrict__ offsets, const uint32_t *count, uint32_t max_count,
     uint2 *__restrict__ pairs, uint32_t max_pairs, uint32_t tiles_x, const Ctrl *ctrl, Ctrl *sort_ctrl,
     uint32_t key_passes) {
-    __shared__ uint32_t s_incl[kBinThreads];
-    __shared__ uint4 s_info[kBinThreads];
     __shared__ uint32_t s_hist[4][256];
-    const uint32_t tid = threadIdx.x;
+    const uint32_t tid = threadIdx.x, lane = tid & 31u;
     const uint32_t n = count ? min(*count, max_count) : max_count;
-    const uint32_t k0 = blockIdx.x * kBinThreads;
-    if (k0 >= n) return;
+    if (blockIdx.x * kBinThreads >= n) return;
     for (uint32_t i = tid; i < 4 * 256; i += kBinThreads) (&s_hist[0][0])[i] = 0u;
+    __syncthreads();
     const uint32_t seg_total = ctrl->seg_total;
-    const uint32_t first = offsets[k0];
-    const uint32_t k = k0 + tid;
-    // inclusive count of this rank, relative to the CTA's first pair
-    const uint32_t next = (k + 1 < n) ? offsets[k + 1] : seg_total;
-    s_incl[tid] = (k < n) ? next - first : 0u;
-    if (k < n) s_info[tid] = info[k];
-    __syncthreads();
-    const uint32_t last = min(kBinThreads, n - k0) - 1;
-    const uint32_t block_pairs = s_incl[last];
-    for (uint32_t t = last + 1 + tid; t < kBinThreads; t += kBinThreads) s_incl[t] = block_pairs;
-    __syncthreads();
-    const uint64_t out0 = (uint64_t)ctrl->pair_base + first;
-    for (uint32_t j = tid; j < block_pairs; j += kBinThreads) {
-        uint32_t lo = 0, hi = kBinThreads - 1;
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (s_incl[mid] > j) hi = mid; else lo = mid + 1;
-        }
-        const uint32_t owner = lo;
-        uint32_t r = j - (owner ? s_incl[owner - 1] : 0u);
-        const uint4 in = s_info[owner];
-        if (in.z) {  // position of the r-th kept tile in the rectangle
-            uint32_t m = in.z;
-            for (uint32_t i = 0; i < r; ++i) m &= m - 1u;
-            r = (uint32_t)(__ffs(m) - 1);
-        }
-        const uint32_t ww = in.y & 0xFFFFu;
-        const uint32_t t = ((in.x >> 16) + r / ww) * tiles_x + (in.x & 0xFFFFu) + r % ww;
-        const uint64_t o = out0 + j;
-        if (o < max_pairs) {
-            pairs[o] = make_uint2(t, in.w);
+    const uint64_t pair_base = ctrl->pair_base;
+    auto emit = [&](uint32_t t, uint32_t value, uint64_t at) {
+        if (at < max_pairs) {
+            pairs[at] = make_uint2(t, value);
             for (uint32_t p = 0; p < key_passes; ++p) atomicAdd(&s_hist[p][(t >> (8u * p)) & 255u], 1u);
+        }
+    };
+    for (uint32_t k0 = blockIdx.x * kBinThreads; k0 < n; k0 += gridDim.x * kBinThreads) {
+        const uint32_t k = k0 + tid;
+        uint4 in = make_uint4(0u, 0u, 0u, 0u);
+        uint32_t cnt = 0;
+        uint64_t o = 0;
+        if (k < n) {
+            in = info[k];
+            const uint32_t off = offsets[k];
+            const uint32_t next = (k + 1 < n) ? offsets[k + 1] : seg_total;
+            cnt = next - off;
+            o = pair_base + off;
+        }
+        const uint32_t x0 = in.x & 0xFFFFu, y0 = in.x >> 16, w = in.y & 0xFFFFu, h = in.y >> 16;
+        if (cnt > 0 && cnt <= kWarpEmit) {
+            // in.z: tiles kept of a rectangle of at most 16 (bit ty·w + tx); 0 = the whole rectangle
+            uint32_t r = 0;
+            for (uint32_t ty = 0; ty < h; ++ty)
+                for (uint32_t tx = 0; tx < w; ++tx)
+                    if (in.z == 0u || ((in.z >> (ty * w + tx)) & 1u)) {
+                        emit((y0 + ty) * tiles_x + x0 + tx, in.w, o + r);
+                        ++r;
+                    }
+        }
+        // Large rectangles (never masked: masks cover at most 16 tiles), one splat at a time.
+        uint32_t big = __ballot_sync(0xFFFFFFFFu, cnt > kWarpEmit);
+        while (big) {
+            const int src = __ffs(big) - 1;
+            big &= big - 1u;
+            const uint32_t bx0 = __shfl_sync(0xFFFFFFFFu, x0, src), by0 = __shfl_sync(0xFFFFFFFFu, y0, src);
+            const uint32_t bw = __shfl_sync(0xFFFFFFFFu, w, src), bcnt = __shfl_sync(0xFFFFFFFFu, cnt, src);
+            const uint32_t bval = __shfl_sync(0xFFFFFFFFu, in.w, src);
+            const uint32_t olo = __shfl_sync(0xFFFFFFFFu, (uint32_t)o, src);
+            const uint32_t ohi = __shfl_sync(0xFFFFFFFFu, (uint32_t)(o >> 32), src);
+            const uint64_t bo = ((uint64_t)ohi << 32) | olo;
+            for (uint32_t r = lane; r < bcnt; r += 32) {
+                const uint32_t ty = r / bw, tx = r - ty * bw;
+                emit((by0 + ty) * tiles_x + bx0 + tx, bval, bo + r);
+            }
         }
     }
     __syncthreads();
@@ -717,8 +734,8 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
                                                          u.std_dev * u.std_dev, L.info, L.offsets);
         const uint32_t scan_blocks = (g.max_count + kScanTile - 1) / kScanTile;
         bin_scan_kernel<<<scan_blocks, 256, 0, st>>>(L.offsets, g.count, g.max_count, L.ctrl, L.flags);
-        bin_emit_kernel<<<blocks, kBinThreads, 0, st>>>(L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs,
-                                                        L.tiles_x, L.ctrl, sort_ctrl, key_passes);
+        bin_emit_kernel<<<blocks < 152 * 8 ? blocks : 152 * 8, kBinThreads, 0, st>>>(
+            L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs, L.tiles_x, L.ctrl, sort_ctrl, key_passes);
         bin_advance_kernel<<<1, 1, 0, st>>>(L.ctrl, g.count, g.max_count, max_pairs);
         count_launches(4);
         rank_offset += g.max_count;
