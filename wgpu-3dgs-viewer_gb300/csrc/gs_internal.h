@@ -73,7 +73,7 @@ struct Tuning {
     uint32_t sort_match = 1;        // depth sort: 1 = match.any ranking, 0 = a ballot per digit bit
     uint32_t hist_blocks = 0;       // depth sort: key-histogram grid (0 = by key count, <= 1216)
 };
-// The defaults, with GS300_SUFFIX_MIN / GS300_SUFFIX_EPS overriding the raster knobs.
+// The defaults, with GS300_SUFFIX_MIN / GS300_SUFFIX_EPS / GS300_HIST_BLOCKS overriding them.
 Tuning default_tuning();
 
 // ---- K2 onesweep radix sort (gs_sort.cu) ----

@@ -379,7 +379,7 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
 
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage, const Tuning *tuning) {
-    const Tuning tn = tuning ? *tuning : Tuning{};
+    const Tuning tn = tuning ? *tuning : default_tuning();
     const uint32_t npasses = sort_passes(key_bits);
     const SortLayout L = sort_layout(scratch, max_count, npasses);
     ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1);
