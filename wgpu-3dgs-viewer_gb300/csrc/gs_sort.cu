@@ -232,14 +232,17 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t invalid = (tile == ntiles - 1) ? ntiles * kTileKeys - n : 0u;
     // Padding keys (all ones) rank last, in the largest digit.
     const uint32_t pub = (d == dmask) ? total - invalid : total;
+    // Digits above dmask hold no key (padding keys sit in digit dmask), so only live digits
+    // publish and look back: a pass over 5 live bits touches 32 flags per block, not 256.
+    const bool live = d <= dmask;
     uint64_t *f = flags + (size_t)tile * 256u + d;
-    st_relaxed(f, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
+    if (live) st_relaxed(f, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
 
     uint32_t blk_total, hist_total;
     const uint32_t start = block_scan_excl(total, s_tmp, &blk_total);
     const uint32_t goff = block_scan_excl(ctrl->hist[pass][d], s_tmp, &hist_total);
     uint32_t prefix = 0;
-    if (tile > 0) {
+    if (tile > 0 && live) {
         prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status);
         st_relaxed(f, pack_flag(epoch, kFlagPrefix, prefix + pub));
     }
