@@ -82,8 +82,15 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage = kProfDepthSort,
                         const Tuning *tuning = nullptr);
 
+// Digits of the packed-pair sort: the key's bits spread evenly over the fewest passes of at
+// most 8 bits (13 bits -> 7 + 6), pass p taking bits [shift[p], shift[p] + bits[p]).
+struct PassSplit {
+    uint32_t shift[4], bits[4], n;
+};
+PassSplit even_split(uint32_t key_bits);
+
 // Packed (uint2 {key, value}) in-place sort for internal pair lists whose digit histograms
-// the producer accumulated into the control block after sort_pairs_begin().
+// (split by even_split) the producer accumulated into the control block after sort_pairs_begin().
 size_t sort_pairs_scratch_bytes(uint32_t max_count, uint32_t key_bits);
 Ctrl *sort_pairs_ctrl(void *scratch);
 cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st);

@@ -32,9 +32,17 @@ struct RasterLayout {
     uint64_t *flags;     // scan look-back flags
     uint2 *pairs;        // (tile, value), capacity max_pairs
     uint2 *ranges;       // per tile [start, end)
+    uint32_t *counts;    // per tile pair count (counting path; null above kCountTiles tiles)
+    uint32_t *blockcounts;  // per emit CTA and tile pair count (counting path)
     void *sort_scratch;
     uint32_t tiles_x, tiles_y, ntiles, key_bits;
 };
+
+// Up to kCountTiles tiles (1080p has 8160), the emit kernel counts pairs per tile in shared
+// memory; the per-tile counts give the tile-sort histograms and, scanned, the tile ranges.
+// Larger targets count per digit instead and find the ranges in the sorted pairs.
+constexpr uint32_t kCountTiles = 8192;
+constexpr uint32_t kEmitBlocks = 152 * 8;
 
 constexpr uint32_t kScanItems = 16;
 constexpr uint32_t kScanTile = 256 * kScanItems;
@@ -71,6 +79,13 @@ static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w
     p += align_up((size_t)max_pairs * 8, 256);
     L.ranges = reinterpret_cast<uint2 *>(p);
     p += align_up((size_t)L.ntiles * sizeof(uint2), 256);
+    L.counts = L.blockcounts = nullptr;
+    if (L.ntiles <= kCountTiles) {
+        L.counts = reinterpret_cast<uint32_t *>(p);
+        p += align_up((size_t)L.ntiles * 4, 256);
+        L.blockcounts = reinterpret_cast<uint32_t *>(p);
+        p += align_up((size_t)kEmitBlocks * L.ntiles * 4, 256);
+    }
     L.sort_scratch = p;
     return L;
 }
@@ -81,7 +96,10 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_
     return align_up(sizeof(Ctrl), 256) + align_up((size_t)max_splats * sizeof(gs_splat), 256) +
            align_up((size_t)max_splats * 16, 256) + align_up((size_t)max_splats * 4 + 16, 256) +
            scan_flag_bytes(max_splats) + align_up((size_t)max_pairs * 8, 256) +
-           align_up((size_t)tiles * sizeof(uint2), 256) + sort_pairs_scratch_bytes(max_pairs, key_bits);
+           align_up((size_t)tiles * sizeof(uint2), 256) +
+           (tiles <= kCountTiles ? align_up((size_t)tiles * 4, 256) + align_up((size_t)kEmitBlocks * tiles * 4, 256)
+                                 : 0) +
+           sort_pairs_scratch_bytes(max_pairs, key_bits);
 }
 
 const Ctrl *raster_ctrl(const void *scratch) { return reinterpret_cast<const Ctrl *>(scratch); }
@@ -300,22 +318,29 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
 // which keeps the global atomics on those few hundred bins to a few per CTA.
 constexpr uint32_t kWarpEmit = 32;
 
+template <bool COUNTS>
 __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
     const uint4 *__restrict__ info, const uint32_t *__restrict__ offsets, const uint32_t *count, uint32_t max_count,
-    uint2 *__restrict__ pairs, uint32_t max_pairs, uint32_t tiles_x, const Ctrl *ctrl, Ctrl *sort_ctrl,
-    uint32_t key_passes) {
-    __shared__ uint32_t s_hist[4][256];
+    uint2 *__restrict__ pairs, uint32_t max_pairs, uint32_t tiles_x, uint32_t ntiles, const Ctrl *ctrl,
+    Ctrl *sort_ctrl, const PassSplit split, uint32_t *__restrict__ blockcounts) {
+    // COUNTS: one counter per tile; else the tile-key digit histograms of the tile sort
+    extern __shared__ uint32_t s_bins[];
+    const uint32_t nbins = COUNTS ? ntiles : 4u * 256u;
     const uint32_t tid = threadIdx.x, lane = tid & 31u;
     const uint32_t n = count ? min(*count, max_count) : max_count;
-    if (blockIdx.x * kBinThreads >= n) return;
-    for (uint32_t i = tid; i < 4 * 256; i += kBinThreads) (&s_hist[0][0])[i] = 0u;
+    for (uint32_t i = tid; i < nbins; i += kBinThreads) s_bins[i] = 0u;
     __syncthreads();
     const uint32_t seg_total = ctrl->seg_total;
     const uint64_t pair_base = ctrl->pair_base;
     auto emit = [&](uint32_t t, uint32_t value, uint64_t at) {
         if (at < max_pairs) {
             pairs[at] = make_uint2(t, value);
-            for (uint32_t p = 0; p < key_passes; ++p) atomicAdd(&s_hist[p][(t >> (8u * p)) & 255u], 1u);
+            if constexpr (COUNTS) {
+                atomicAdd(&s_bins[t], 1u);
+            } else {
+                for (uint32_t p = 0; p < split.n; ++p)
+                    atomicAdd(&s_bins[p * 256u + ((t >> split.shift[p]) & ((1u << split.bits[p]) - 1u))], 1u);
+            }
         }
     };
     for (uint32_t k0 = blockIdx.x * kBinThreads; k0 < n; k0 += gridDim.x * kBinThreads) {
@@ -359,10 +384,85 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
         }
     }
     __syncthreads();
-    for (uint32_t p = 0; p < key_passes; ++p) {
-        const uint32_t v = s_hist[p][tid];
-        if (v) atomicAdd(&sort_ctrl->hist[p][tid], v);
+    if constexpr (COUNTS) {
+        // every CTA of the grid writes its slice (zeros when it had no ranks): plain stores,
+        // summed per tile by tile_count_kernel
+        uint32_t *dst = blockcounts + (size_t)blockIdx.x * ntiles;
+        for (uint32_t t = tid; t < ntiles; t += kBinThreads) dst[t] = s_bins[t];
+    } else {
+        for (uint32_t p = 0; p < split.n; ++p) {
+            const uint32_t v = s_bins[p * 256u + tid];
+            if (v) atomicAdd(&sort_ctrl->hist[p][tid], v);
+        }
     }
+}
+
+// Per-tile pair counts of one segment (the sum over the emit CTAs), added to the running
+// counts.  blockIdx.y takes a slice of the emit CTAs, so the sum runs wide, not long.
+constexpr uint32_t kCountSlices = 16;
+
+__global__ void __launch_bounds__(256) tile_count_kernel(const uint32_t *__restrict__ blockcounts, uint32_t nblocks,
+                                                         uint32_t ntiles, uint32_t *__restrict__ counts) {
+    const uint32_t t = blockIdx.x * 256u + threadIdx.x;
+    if (t >= ntiles) return;
+    const uint32_t per = (nblocks + kCountSlices - 1) / kCountSlices;
+    const uint32_t b0 = blockIdx.y * per, b1 = min(nblocks, b0 + per);
+    uint32_t part[4] = {0, 0, 0, 0};
+    uint32_t b = b0;
+    for (; b + 4 <= b1; b += 4)
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) part[q] += blockcounts[(size_t)(b + q) * ntiles + t];
+    for (; b < b1; ++b) part[0] += blockcounts[(size_t)b * ntiles + t];
+    const uint32_t c = (part[0] + part[1]) + (part[2] + part[3]);
+    if (c) atomicAdd(&counts[t], c);
+}
+
+// [start, end) of every tile from the per-tile counts (exclusive scan; one CTA, 8 tiles a
+// thread), and the tile-sort digit histograms, which are sums of those counts.
+__global__ void __launch_bounds__(1024) tile_scan_kernel(const uint32_t *__restrict__ counts, uint32_t ntiles,
+                                                         uint2 *__restrict__ ranges, Ctrl *sort_ctrl,
+                                                         const PassSplit split) {
+    __shared__ uint32_t s_w[32];
+    __shared__ uint32_t s_h[4][256];
+    const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+    (&s_h[0][0])[tid] = 0u;
+    __syncthreads();
+    const uint32_t base = tid * 8u;
+    uint32_t v[8], sum = 0;
+#pragma unroll
+    for (uint32_t j = 0; j < 8; ++j) {
+        v[j] = base + j < ntiles ? counts[base + j] : 0u;
+        sum += v[j];
+        if (v[j])
+            for (uint32_t p = 0; p < split.n; ++p)
+                atomicAdd(&s_h[p][((base + j) >> split.shift[p]) & ((1u << split.bits[p]) - 1u)], v[j]);
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= o) inc += x;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t x = s_w[lane], xi = x;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, xi, o);
+            if (lane >= o) xi += y;
+        }
+        s_w[lane] = xi - x;  // exclusive over warps
+    }
+    __syncthreads();
+    uint32_t run = s_w[warp] + inc - sum;
+#pragma unroll
+    for (uint32_t j = 0; j < 8; ++j) {
+        if (base + j < ntiles) ranges[base + j] = make_uint2(run, run + v[j]);
+        run += v[j];
+    }
+    const uint32_t p = tid >> 8, d = tid & 255u;
+    if (p < split.n) sort_ctrl->hist[p][d] = s_h[p][d];
 }
 
 // K3d: advance the running pair base past a segment; flags a tile-pair list overflow.
@@ -718,7 +818,11 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     cudaError_t e = sort_pairs_begin(L.sort_scratch, st);
     if (e != cudaSuccess) return e;
     Ctrl *sort_ctrl = sort_pairs_ctrl(L.sort_scratch);
-    const uint32_t key_passes = (L.key_bits + 7u) / 8u;
+    if (L.counts) {
+        e = cudaMemsetAsync(L.counts, 0, (size_t)L.ntiles * 4, st);
+        if (e != cudaSuccess) return e;
+    }
+    const PassSplit split = even_split(L.key_bits);
     uint32_t rank_offset = 0;
     prof_mark(kProfBin, true, st);
     const int direct = nseg == 1 ? 1 : 0;
@@ -735,11 +839,26 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
                                                          u.std_dev * u.std_dev, L.info, L.offsets);
         const uint32_t scan_blocks = (g.max_count + kScanTile - 1) / kScanTile;
         bin_scan_kernel<<<scan_blocks, 256, 0, st>>>(L.offsets, g.count, g.max_count, L.ctrl, L.flags);
-        bin_emit_kernel<<<blocks < 152 * 8 ? blocks : 152 * 8, kBinThreads, 0, st>>>(
-            L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs, L.tiles_x, L.ctrl, sort_ctrl, key_passes);
+        const uint32_t eblocks = blocks < kEmitBlocks ? blocks : kEmitBlocks;
+        if (L.counts) {
+            bin_emit_kernel<true><<<eblocks, kBinThreads, L.ntiles * 4u, st>>>(
+                L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs, L.tiles_x, L.ntiles, L.ctrl, sort_ctrl,
+                split, L.blockcounts);
+            tile_count_kernel<<<dim3((L.ntiles + 255) / 256, kCountSlices), 256, 0, st>>>(L.blockcounts, eblocks,
+                                                                                         L.ntiles, L.counts);
+            count_launches(1);
+        } else {
+            bin_emit_kernel<false><<<eblocks, kBinThreads, 4u * 256u * 4u, st>>>(
+                L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs, L.tiles_x, L.ntiles, L.ctrl, sort_ctrl,
+                split, nullptr);
+        }
         bin_advance_kernel<<<1, 1, 0, st>>>(L.ctrl, g.count, g.max_count, max_pairs);
         count_launches(4);
         rank_offset += g.max_count;
+    }
+    if (L.counts) {
+        tile_scan_kernel<<<1, 1024, 0, st>>>(L.counts, L.ntiles, L.ranges, sort_ctrl, split);
+        count_launches(1);
     }
     prof_mark(kProfBin, false, st);
     prof_mark(kProfTileSort, true, st);
@@ -748,15 +867,17 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
     if (e != cudaSuccess) return e;
     merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, sort_ctrl);
     count_launches(1);
-    e = cudaMemsetAsync(L.ranges, 0, (size_t)L.ntiles * sizeof(uint2), st);
-    if (e != cudaSuccess) return e;
-    uint32_t rblocks = (max_pairs + 255) / 256;
-    if (rblocks > 152 * 8) rblocks = 152 * 8;
-    if (rblocks == 0) rblocks = 1;
-    prof_mark(kProfRanges, true, st);
-    tile_ranges_kernel<<<rblocks, 256, 0, st>>>(L.pairs, L.ctrl, L.ranges, L.ntiles);
-    prof_mark(kProfRanges, false, st);
-    count_launches(1);
+    if (!L.counts) {  // more tiles than the counting path covers: ranges from the sorted pairs
+        prof_mark(kProfRanges, true, st);
+        e = cudaMemsetAsync(L.ranges, 0, (size_t)L.ntiles * sizeof(uint2), st);
+        if (e != cudaSuccess) return e;
+        uint32_t rblocks = (max_pairs + 255) / 256;
+        if (rblocks > 152 * 8) rblocks = 152 * 8;
+        if (rblocks == 0) rblocks = 1;
+        tile_ranges_kernel<<<rblocks, 256, 0, st>>>(L.pairs, L.ctrl, L.ranges, L.ntiles);
+        prof_mark(kProfRanges, false, st);
+        count_launches(1);
+    }
     const float std2 = u.std_dev * u.std_dev;
     const float o = u.std_dev - 0.1f;
     const float outline2 = o * o;

@@ -155,7 +155,7 @@ template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
 __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
-    uint32_t max_count, uint32_t pass, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags) {
+    uint32_t max_count, uint32_t pass, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags) {
     __shared__ uint2 s_kv[kTileKeys];
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_start[256];
@@ -174,7 +174,6 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t ntiles = (n + kTileKeys - 1) / kTileKeys;
     const uint32_t tile = s_tile, epoch = s_epoch;
     if (tile >= ntiles) return;
-    const uint32_t shift = 8u * pass;
     const uint32_t dmask = (1u << digit_bits) - 1u;  // bits above the key width are ignored
     const uint32_t base = tile * kTileKeys + warp * (32u * kSortRows);
 
@@ -301,6 +300,19 @@ __global__ void copy_packed_kernel(const uint2 *src, uint2 *dst, const uint32_t 
 static inline uint32_t sort_passes(uint32_t key_bits) { return (key_bits + 7u) / 8u; }
 // Live bits of pass p's digit: keys are below 2^key_bits.  Invalid (padding) keys are all ones
 // but sort last either way, because they hold the largest value in every live bit.
+PassSplit even_split(uint32_t key_bits) {
+    PassSplit sp{};
+    sp.n = sort_passes(key_bits);
+    const uint32_t base = sp.n ? key_bits / sp.n : 0u, extra = sp.n ? key_bits % sp.n : 0u;
+    uint32_t at = 0;
+    for (uint32_t p = 0; p < sp.n; ++p) {
+        sp.shift[p] = at;
+        sp.bits[p] = base + (p < extra ? 1u : 0u);
+        at += sp.bits[p];
+    }
+    return sp;
+}
+
 static inline uint32_t pass_bits(uint32_t key_bits, uint32_t p) {
     const uint32_t left = key_bits - 8u * p;
     return left < 8u ? left : 8u;
@@ -358,25 +370,25 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
     const size_t fstride = (size_t)L.ntiles * 256;
     if (npasses == 1) {
         sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
+            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags);
         unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
         count_launches(2);
         return;
     }
     uint2 *src = L.alt_a, *dst = L.alt_b;
     sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, pass_bits(key_bits, 0), L.ctrl, L.flags);
+        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags);
     for (uint32_t p = 1; p + 1 < npasses; ++p) {
         sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, pass_bits(key_bits, p), L.ctrl,
+            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, 8u * p, pass_bits(key_bits, p), L.ctrl,
             L.flags + p * fstride);
         uint2 *t = src;
         src = dst;
         dst = t;
     }
     sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, pass_bits(key_bits, npasses - 1),
-        L.ctrl, L.flags + (npasses - 1) * fstride);
+        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, 8u * (npasses - 1),
+        pass_bits(key_bits, npasses - 1), L.ctrl, L.flags + (npasses - 1) * fstride);
     count_launches(npasses);
 }
 
@@ -415,12 +427,13 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
     const uint32_t npasses = sort_passes(key_bits);
     if (max_count == 0) return cudaSuccess;
     SortLayout L = sort_layout(scratch, max_count, 1);
+    const PassSplit split = even_split(key_bits);
     const size_t fstride = (size_t)L.ntiles * 256;
     uint2 *src = data, *dst = L.alt_a;
     for (uint32_t p = 0; p < npasses; ++p) {
         sort_pass_kernel<true, true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
-                                                                       count, max_count, p, pass_bits(key_bits, p), L.ctrl,
-                                                                       L.flags + p * fstride);
+                                                                              count, max_count, p, split.shift[p],
+                                                                              split.bits[p], L.ctrl, L.flags + p * fstride);
         uint2 *t = src;
         src = dst;
         dst = t;
