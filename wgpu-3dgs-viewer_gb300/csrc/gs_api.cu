@@ -138,6 +138,7 @@ struct DevBuf {
 
 gs_status status_from_bits(uint32_t bits, const char *what) {
     if (bits & kStatusTimeout) return fail(GS_ERR_TIMEOUT, "%s: a bounded device wait gave up", what);
+    if (bits & kStatusBounds) return fail(GS_ERR_CUDA, "%s: a device index check failed", what);
     if (bits & kStatusCapacity) return fail(GS_ERR_CAPACITY, "%s: tile-pair list exceeded its capacity", what);
     return GS_OK;
 }
@@ -726,7 +727,7 @@ gs_status gs_viewer_synchronize(gs_viewer *v, gs_stream stream) {
         Ctrl c{};
         GS_CUDA(cudaMemcpy(&c, v->frame.raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
         const uint32_t bits = c.status | v->model.device_status();
-        if (bits & kStatusTimeout) return status_from_bits(bits, "render");
+        if (bits & (kStatusTimeout | kStatusBounds)) return status_from_bits(bits, "render");
         if (!(bits & kStatusCapacity)) return GS_OK;
         gs_status s = v->frame.grow_pairs(c.total);
         if (s != GS_OK) return s;
@@ -991,7 +992,7 @@ gs_status gs_multi_viewer_synchronize(gs_multi_viewer *v, gs_stream stream) {
             auto it = v->models.find(k);
             if (it != v->models.end()) bits |= it->second->device_status();
         }
-        if (bits & kStatusTimeout) return status_from_bits(bits, "render");
+        if (bits & (kStatusTimeout | kStatusBounds)) return status_from_bits(bits, "render");
         if (!(bits & kStatusCapacity)) return GS_OK;
         gs_status s = v->frame.grow_pairs(c.total);
         if (s != GS_OK) return s;
@@ -1285,7 +1286,7 @@ gs_status gs_batch_synchronize(gs_batch *b, gs_stream stream) {
                                        cudaMemcpyDeviceToHost));
                     bits |= gc.status;
                 }
-            if (bits & kStatusTimeout) return status_from_bits(bits, "batch");
+            if (bits & (kStatusTimeout | kStatusBounds)) return status_from_bits(bits, "batch");
             if (bits & kStatusCapacity) {
                 uint64_t p = (uint64_t)c.total + c.total / 4 + 4096;
                 v.max_pairs = p > 0x7FFFFFFFull ? 0x7FFFFFFFu : (uint32_t)p;
@@ -1390,9 +1391,12 @@ gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n,
             GS_CUDA(cudaStreamSynchronize(st));
             bool regrow = false;
             for (uint32_t i = 0; i < n; ++i) {
-                Ctrl c{};
+                Ctrl c{}, a{}, q{};
                 GS_CUDA(cudaMemcpy(&c, b->slots[i].raster_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
-                if (c.status & kStatusTimeout) return status_from_bits(c.status, "autotune");
+                GS_CUDA(cudaMemcpy(&a, b->slots[i].pre_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+                GS_CUDA(cudaMemcpy(&q, b->slots[i].sort_scratch.ptr, sizeof(Ctrl), cudaMemcpyDeviceToHost));
+                const uint32_t bad = (c.status | a.status | q.status) & (kStatusTimeout | kStatusBounds);
+                if (bad) return status_from_bits(bad, "autotune");
                 if (c.status & kStatusCapacity) {
                     uint64_t p = (uint64_t)c.total + c.total / 4 + 4096;
                     b->slots[i].max_pairs = p > 0x7FFFFFFFull ? 0x7FFFFFFFu : (uint32_t)p;

@@ -11,6 +11,7 @@ namespace gs {
 // Sticky error bits of a scratch area's control block.
 constexpr uint32_t kStatusTimeout = 1u;
 constexpr uint32_t kStatusCapacity = 2u;
+constexpr uint32_t kStatusBounds = 4u;  // an index check failed; the access was skipped
 
 // Upper bound on polls of a look-back flag or an mbarrier before a kernel gives up, records
 // kStatusTimeout and carries on with a garbage value (so that waiting successors also end).

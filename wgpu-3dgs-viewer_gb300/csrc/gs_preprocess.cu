@@ -584,14 +584,19 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     }
     __syncthreads();
     if (tile == P.ntiles - 1) {
-        const uint32_t v = P.ctrl->count;
+        const uint32_t v = min(P.ctrl->count, P.depth_cap);
         const uint32_t padded = min(((v + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS) * GS_SORT_BLOCK_KVS, P.depth_cap);
         for (uint32_t k = v + tid; k < padded; k += kPreThreads) P.depths[k] = 2.0f;
     }
     if (vis) {
+        // c < n unless a look-back gave up (status already set); never write past the buffers
         const uint32_t c = s_base + s_warp[warp] + __popc(bal & lanemask_lt());
-        P.indices[c] = i;
-        P.depths[c] = key;
+        if (c < P.n) {
+            P.indices[c] = i;
+            P.depths[c] = key;
+        } else {
+            atomicOr(&P.ctrl->status, kStatusBounds);
+        }
     }
 }
 
@@ -686,7 +691,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
     for (uint32_t v = 0; v < nv; ++v) {
         const PreView &V = P.views[v];
         if (tile == P.ntiles - 1) {
-            const uint32_t c = V.ctrl->count;
+            const uint32_t c = min(V.ctrl->count, V.depth_cap);
             const uint32_t padded = min(((c + GS_SORT_BLOCK_KVS - 1) / GS_SORT_BLOCK_KVS) * GS_SORT_BLOCK_KVS, V.depth_cap);
             for (uint32_t k = c + tid; k < padded; k += kPreThreads) V.depths[k] = 2.0f;
         }
@@ -695,8 +700,12 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
             uint32_t off = s_base[v];
             for (uint32_t w = 0; w < warp; ++w) off += __popc(s_bal[v][w]);
             const uint32_t c = off + __popc(bal & lt);
-            V.indices[c] = i;
-            V.depths[c] = s_key[v][tid];
+            if (c < P.n) {
+                V.indices[c] = i;
+                V.depths[c] = s_key[v][tid];
+            } else {
+                atomicOr(&V.ctrl->status, kStatusBounds);
+            }
         }
     }
 }

@@ -336,7 +336,8 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
         if (at < max_pairs) {
             pairs[at] = make_uint2(t, value);
             if constexpr (COUNTS) {
-                atomicAdd(&s_bins[t], 1u);
+                if (t < ntiles) atomicAdd(&s_bins[t], 1u);
+                else atomicOr(&const_cast<Ctrl *>(ctrl)->status, kStatusBounds);
             } else {
                 for (uint32_t p = 0; p < split.n; ++p)
                     atomicAdd(&s_bins[p * 256u + ((t >> split.shift[p]) & ((1u << split.bits[p]) - 1u))], 1u);
@@ -608,14 +609,19 @@ template <uint32_t MODE, bool PORTABLE_EXP, bool COUNT>
 __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
     const gs_splat *__restrict__ sorted, const uint2 *__restrict__ pairs, const uint2 *__restrict__ ranges,
     uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch, uint32_t tiles_x, float std2,
-    float outline2, uint32_t max_splats, uint32_t suffix_min, float eps, unsigned long long *counters) {
+    float outline2, uint32_t max_splats, uint32_t suffix_min, float eps, unsigned long long *counters,
+    Ctrl *pctrl) {
     __shared__ RasterShared S;
     // Work tallies of the counting variant (profiling only): fragment evaluations, alphas,
     // channel-triple blends and transmittance updates.
     uint32_t n_eval = 0, n_alpha = 0, n_blend = 0, n_trans = 0;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    const uint2 range = ranges[blockIdx.x];
+    uint2 range = ranges[blockIdx.x];
+    if (range.y < range.x || range.y > pctrl->count) {
+        if (threadIdx.x == 0) atomicOr(&pctrl->status, kStatusBounds);
+        range = make_uint2(0u, 0u);
+    }
     const uint32_t s0 = range.x, n = range.y - range.x;
     const uint32_t wx0 = tx * GS_TILE + (warp & 1u) * 8u, wy0 = ty * GS_TILE + (warp >> 1) * 4u;
     const uint32_t px = wx0 + (lane & 7u), py = wy0 + (lane >> 3);
@@ -791,17 +797,17 @@ static void launch_raster_mode(const RasterLayout &L, const gs_splat *splats, ui
     if (exact) {
         raster_kernel<MODE, true, false><<<L.ntiles, kRasterThreads, 0, st>>>(
             splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
-            nullptr);
+            nullptr, L.ctrl);
     } else if (MODE == GS_DISPLAY_SPLAT && prof_enabled()) {
         unsigned long long *counts = nullptr;
         cudaGetSymbolAddress((void **)&counts, g_raster_counts);
         raster_kernel<GS_DISPLAY_SPLAT, false, true><<<L.ntiles, kRasterThreads, 0, st>>>(
             splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
-            counts);
+            counts, L.ctrl);
     } else {
         raster_kernel<MODE, false, false><<<L.ntiles, kRasterThreads, 0, st>>>(
             splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
-            nullptr);
+            nullptr, L.ctrl);
     }
 }
 

@@ -253,7 +253,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
 #pragma unroll
         for (uint32_t i = 0; i < kSortRows; ++i) {
             const uint32_t dd = (k[i] >> shift) & dmask;
-            s_kv[s_start[dd] + s_whist[warp][dd] + r[i]] = make_uint2(k[i], v[i]);
+            const uint32_t at = s_start[dd] + s_whist[warp][dd] + r[i];
+            if (at < kTileKeys) s_kv[at] = make_uint2(k[i], v[i]);
+            else atomicOr(&ctrl->status, kStatusBounds);
         }
     } else {
         // Values are read only now, after ranking, which keeps them out of registers above.
@@ -262,7 +264,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
             const uint32_t pos = base + i * 32u + lane;
             const uint32_t vv = pos < n ? vin[pos] : 0u;
             const uint32_t dd = (k[i] >> shift) & dmask;
-            s_kv[s_start[dd] + s_whist[warp][dd] + r[i]] = make_uint2(k[i], vv);
+            const uint32_t at = s_start[dd] + s_whist[warp][dd] + r[i];
+            if (at < kTileKeys) s_kv[at] = make_uint2(k[i], vv);
+            else atomicOr(&ctrl->status, kStatusBounds);
         }
     }
     __syncthreads();
