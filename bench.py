@@ -468,8 +468,8 @@ def main():
         "depth_sort": 68.0 * V,
         # sorted index read, splat gathered and written in draw order, (tile, rank) pairs written
         "bin": V * (4 + 2 * SPLAT_BYTES) + 8.0 * P,
-        # 2 passes over (tile, rank) pairs + key histogram read
-        "tile_sort": 36.0 * P,
+        # 2 passes over (tile, value) pairs (digit histograms come from the per-tile counts)
+        "tile_sort": 32.0 * P,
         "ranges": 4.0 * P,
         # pair ranks + splat records read per pair, frame written
         "raster": P * (4 + SPLAT_BYTES) + 4.0 * W * H,

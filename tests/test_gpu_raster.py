@@ -102,3 +102,36 @@ def test_early_out_paths_bit_exact(gs, cuda, oracle, monkeypatch, suffix_min, ep
     got = pipe.render(u)
     want = _oracle_frame(oracle, u, sc, R.FORMAT_FP32, w, h, exp_mode=0, threads=8)
     assert np.array_equal(got, want), f"{(got != want).any(axis=-1).sum()} pixels differ"
+
+
+@pytest.mark.parametrize("w,h", [(3840, 2160), (2048, 4608)])
+def test_frame_bit_exact_above_8192_tiles(gs, cuda, oracle, monkeypatch, w, h):
+    """Targets with more than 8192 16x16 tiles (4K: 32400) take the other binning path (digit
+    histograms counted at emission, tile ranges found in the sorted pairs, 15-bit tile keys)."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(60_000, seed=23)
+    # 4x the pixels of 1080p: splats cover about 4x the tiles, so the pair list is sized for it
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, w, h, max_pairs=64 * len(sc))
+    u = uniforms(gs, w, h, k=7, radius=5.0)
+    got = pipe.render(u)
+    st, pairs = gs.Renderer.status(pipe.r_scratch)
+    assert st == 0 and pairs > 0
+    want = _oracle_frame(oracle, u, sc, R.FORMAT_FP32, w, h, exp_mode=0, threads=16)
+    assert np.array_equal(got, want), f"{(got != want).any(axis=-1).sum()} pixels differ"
+
+
+def test_viewer_4k_matches_stage_path(gs, cuda, monkeypatch):
+    """The Viewer at 4K (through its own scratch and regrowth) equals the stage-level frame."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(200_000, seed=24)
+    w, h = 3840, 2160
+    v = gs.Viewer(sc)
+    v.update_camera(S.orbit_camera(11, radius=6.0), (w, h))
+    t = gs.RenderTarget(w, h)
+    v.render(t)
+    v.synchronize()
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, w, h, max_pairs=64 * len(sc))
+    u = uniforms(gs, w, h, k=11, radius=6.0)
+    got = pipe.render(u)
+    assert gs.Renderer.status(pipe.r_scratch)[0] == 0
+    assert np.array_equal(t.download(), got)
