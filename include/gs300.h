@@ -392,6 +392,12 @@ gs_status gs_server_submit(gs_server *server, const char *key, const gs_camera_p
 gs_status gs_server_wait(gs_server *server, uint64_t ticket, double timeout_s, double *latency_ms);
 gs_status gs_server_stats(gs_server *server, gs_server_report *out);
 gs_status gs_server_reset_stats(gs_server *server);
+/* Dynamic batching: up to `max_views` (1..16, default 16) admitted requests of one scene share
+ * one preprocess launch that reads the scene's records once; 1 runs every request alone.  With
+ * `max_wait_ms` > 0 (0..1000, default 0), while a scene has more requests queued than slots are
+ * free, admission holds for up to that long (from when the hold began) for busy slots to free up,
+ * so that larger groups form. */
+gs_status gs_server_set_batching(gs_server *server, uint32_t max_views, double max_wait_ms);
 
 #ifdef __cplusplus
 }

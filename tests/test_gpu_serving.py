@@ -64,3 +64,42 @@ def test_admission_by_memory_budget(gs, cuda):
     assert e.value.status == 7  # GS_ERR_ADMISSION
     with pytest.raises(gs.ModelNotFound):
         sv.submit("missing", cam, 640, 360)
+
+
+def test_dynamic_batching_matches_viewer(gs, cuda, monkeypatch):
+    """A burst of requests for one scene is admitted as groups sharing one preprocess launch
+    (up to 16, here limited by 12 slots); every frame equals the Viewer's for that camera."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(80_000, seed=61)
+    mv = gs.MultiModelViewer()
+    mv.insert_model("s", sc)
+    sv = gs.Server(mv, budget_bytes=16 << 30, max_inflight=12)
+    reqs = [(RES[i % 3], S.orbit_camera(7 * i, radius=6.0 + 0.2 * i)) for i in range(20)]
+    outs = [np.zeros((h, w, 4), np.uint8) for (w, h), _ in reqs]
+    tickets = [sv.submit("s", gs.CameraPod.new(cam, (w, h)), w, h, o) for ((w, h), cam), o in zip(reqs, outs)]
+    for t in tickets:
+        sv.wait(t)
+    v = gs.Viewer(sc)
+    for ((w, h), cam), o in zip(reqs, outs):
+        v.update_camera(cam, (w, h))
+        tgt = gs.RenderTarget(w, h)
+        v.render(tgt)
+        v.synchronize()
+        assert np.array_equal(o, tgt.download())
+    sv.set_batching(1)  # every request alone
+    again = [np.zeros((h, w, 4), np.uint8) for (w, h), _ in reqs]
+    tickets = [sv.submit("s", gs.CameraPod.new(cam, (w, h)), w, h, o) for ((w, h), cam), o in zip(reqs, again)]
+    for t in tickets:
+        sv.wait(t)
+    for a, b in zip(outs, again):
+        assert np.array_equal(a, b)
+    sv.set_batching(16, max_wait_ms=2.0)  # batching window
+    third = [np.zeros((h, w, 4), np.uint8) for (w, h), _ in reqs]
+    tickets = [sv.submit("s", gs.CameraPod.new(cam, (w, h)), w, h, o) for ((w, h), cam), o in zip(reqs, third)]
+    for t in tickets:
+        sv.wait(t)
+    for a, b in zip(outs, third):
+        assert np.array_equal(a, b)
+    for bad in ((0, 0.0), (17, 0.0), (4, -1.0), (4, 5000.0)):
+        with pytest.raises(gs.GsError):
+            sv.set_batching(*bad)

@@ -1499,6 +1499,12 @@ struct ServerSlot {
     cudaEvent_t done = nullptr;
     uint64_t req = 0;
     bool busy = false;
+    // Dynamic batching: this slot's uniforms on the device; as a group's leader, the group's
+    // PreView descriptors and control block, and the pinned staging they are copied from.
+    DevBuf u_dev, views_dev, group;
+    gs_frame_uniforms *u_host = nullptr;
+    PreView *views_host = nullptr;
+    cudaEvent_t pre_done = nullptr;
 };
 
 }  // namespace
@@ -1506,6 +1512,9 @@ struct ServerSlot {
 struct gs_server {
     gs_multi_viewer *mv = nullptr;
     size_t budget = 0, reserved = 0;
+    uint32_t batch_views = kPreMaxViews;  // requests of one scene sharing a preprocess launch
+    double batch_wait_ms = 0.0;           // how long admission may hold for more free slots
+    double hold_since = -1.0;             // when the current hold began (-1: not holding)
     std::vector<ServerSlot> slots;
     std::deque<uint64_t> queue;
     std::unordered_map<uint64_t, ServerReq> reqs;
@@ -1530,41 +1539,43 @@ struct gs_server {
                 cudaStreamDestroy(sl.stream);
             }
             if (sl.done) cudaEventDestroy(sl.done);
+            if (sl.pre_done) cudaEventDestroy(sl.pre_done);
+            if (sl.u_host) cudaFreeHost(sl.u_host);
+            if (sl.views_host) cudaFreeHost(sl.views_host);
         }
     }
 };
 
 namespace {
 
-// Enqueue one admitted request on its slot's stream (scheduler thread, server lock held).
-gs_status server_launch(gs_server *sv, ServerReq &r, ServerSlot &sl) {
+// Buffers, target and uniforms of one admitted request (scheduler thread, server lock held).
+gs_status server_prepare(gs_server *sv, ServerReq &r, ServerSlot &sl, uint8_t **target, uint32_t *pitch,
+                         gs_frame_uniforms *u) {
     bool changed = false;
     GS_CUDA(sl.view.prepare(r.model, r.w, r.h, &changed));
-    uint8_t *target = r.out;
-    uint32_t pitch = r.pitch;
+    *target = r.out;
+    *pitch = r.pitch;
     if (r.out_on_host || !r.out) {
         GS_CUDA(sl.target.ensure((size_t)r.w * r.h * 4));
-        target = (uint8_t *)sl.target.ptr;
-        pitch = r.w * 4;
+        *target = (uint8_t *)sl.target.ptr;
+        *pitch = r.w * 4;
     }
     gs_gaussian_transform_pod gt;
     {
         std::lock_guard<std::mutex> g(sv->mv->mu);
         gt = sv->mv->frame.gt;
     }
-    gs_frame_uniforms u;
-    gs_status s = gs_frame_uniforms_build(&r.camera, &r.model->model, &gt, r.w, r.h, &u);
-    if (s != GS_OK) return s;
+    return gs_frame_uniforms_build(&r.camera, &r.model->model, &gt, r.w, r.h, u);
+}
+
+// Depth sort, raster, read-back and completion event of a request whose preprocess is enqueued.
+gs_status server_finish(gs_server *sv, ServerReq &r, ServerSlot &sl, uint8_t *target, uint32_t pitch,
+                        const gs_frame_uniforms &u) {
     const Model *m = r.model;
     ViewSlot &v = sl.view;
     uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
-    cudaError_t e = launch_preprocess(u, m->records.ptr, m->format, m->n,
-                                      m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert, ind,
-                                      ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr, gs_depth_capacity(m->n),
-                                      (gs_splat *)v.splats.ptr, v.pre_scratch.ptr, sl.stream);
-    if (e == cudaSuccess)
-        e = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, 32, v.sort_scratch.ptr,
-                        sl.stream);
+    cudaError_t e = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, 32,
+                                v.sort_scratch.ptr, sl.stream);
     if (e == cudaSuccess) {
         const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
         e = launch_raster(&seg, 1, u, target, r.w, r.h, pitch, v.max_pairs, v.raster_scratch.ptr,
@@ -1574,6 +1585,77 @@ gs_status server_launch(gs_server *sv, ServerReq &r, ServerSlot &sl) {
         e = cudaMemcpyAsync(r.out, target, (size_t)r.w * r.h * 4, cudaMemcpyDeviceToHost, sl.stream);
     if (e == cudaSuccess) e = cudaEventRecord(sl.done, sl.stream);
     if (e != cudaSuccess) return cuda_fail(e, "server launch");
+    return GS_OK;
+}
+
+// Enqueue one admitted request on its slot's stream (scheduler thread, server lock held).
+gs_status server_launch(gs_server *sv, ServerReq &r, ServerSlot &sl) {
+    uint8_t *target;
+    uint32_t pitch;
+    gs_frame_uniforms u;
+    gs_status s = server_prepare(sv, r, sl, &target, &pitch, &u);
+    if (s != GS_OK) return s;
+    const Model *m = r.model;
+    ViewSlot &v = sl.view;
+    uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+    const cudaError_t e = launch_preprocess(u, m->records.ptr, m->format, m->n,
+                                            m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert,
+                                            ind, ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr,
+                                            gs_depth_capacity(m->n), (gs_splat *)v.splats.ptr, v.pre_scratch.ptr,
+                                            sl.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "server launch");
+    return server_finish(sv, r, sl, target, pitch, u);
+}
+
+// Dynamic batching: admitted requests of one scene (group[0] leads) share one preprocess launch
+// that reads the scene's records once; each then sorts, rasterises and completes on its own
+// slot's stream.  The leader slot's staging stays untouched until the leader completes, which is
+// after the shared launch.
+gs_status server_launch_group(gs_server *sv, const std::vector<std::pair<ServerReq *, ServerSlot *>> &group) {
+    if (group.size() == 1) return server_launch(sv, *group[0].first, *group[0].second);
+    ServerSlot &lead = *group[0].second;
+    const Model *m = group[0].first->model;
+    const size_t nv = group.size();
+    if (!lead.views_host) GS_CUDA(cudaMallocHost(&lead.views_host, kPreMaxViews * sizeof(PreView)));
+    GS_CUDA(lead.views_dev.ensure(kPreMaxViews * sizeof(PreView)));
+    if (!lead.group.ptr) {
+        GS_CUDA(lead.group.ensure(align_up(sizeof(Ctrl), 256)));
+        GS_CUDA(cudaMemset(lead.group.ptr, 0, align_up(sizeof(Ctrl), 256)));
+    }
+    if (!lead.pre_done) GS_CUDA(cudaEventCreateWithFlags(&lead.pre_done, cudaEventDisableTiming));
+    std::vector<uint8_t *> targets(nv);
+    std::vector<uint32_t> pitches(nv);
+    std::vector<gs_frame_uniforms> us(nv);
+    for (size_t k = 0; k < nv; ++k) {
+        ServerReq &r = *group[k].first;
+        ServerSlot &sl = *group[k].second;
+        gs_status s = server_prepare(sv, r, sl, &targets[k], &pitches[k], &us[k]);
+        if (s != GS_OK) return s;
+        if (!sl.u_host) GS_CUDA(cudaMallocHost(&sl.u_host, sizeof(gs_frame_uniforms)));
+        GS_CUDA(sl.u_dev.ensure(sizeof(gs_frame_uniforms)));
+        *sl.u_host = us[k];
+        ViewSlot &v = sl.view;
+        uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+        lead.views_host[k] = preprocess_view((const gs_frame_uniforms *)sl.u_dev.ptr, ind, ind + 4,
+                                             (uint32_t *)v.indices.ptr, (float *)v.depths.ptr, gs_depth_capacity(m->n),
+                                             (gs_splat *)v.splats.ptr, v.pre_scratch.ptr);
+        GS_CUDA(cudaMemcpyAsync(sl.u_dev.ptr, sl.u_host, sizeof(gs_frame_uniforms), cudaMemcpyHostToDevice,
+                                lead.stream));
+    }
+    GS_CUDA(cudaMemcpyAsync(lead.views_dev.ptr, lead.views_host, nv * sizeof(PreView), cudaMemcpyHostToDevice,
+                            lead.stream));
+    cudaError_t e = launch_preprocess_views(m->records.ptr, m->format, m->n,
+                                            m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert,
+                                            (const PreView *)lead.views_dev.ptr, (uint32_t)nv, lead.group.ptr,
+                                            lead.stream);
+    if (e == cudaSuccess) e = cudaEventRecord(lead.pre_done, lead.stream);
+    if (e != cudaSuccess) return cuda_fail(e, "server group launch");
+    for (size_t k = 0; k < nv; ++k) {
+        ServerSlot &sl = *group[k].second;
+        if (k > 0) GS_CUDA(cudaStreamWaitEvent(sl.stream, lead.pre_done, 0));
+        const gs_status s = server_finish(sv, *group[k].first, sl, targets[k], pitches[k], us[k]);
+        if (s != GS_OK) return s;
+    }
     return GS_OK;
 }
 
@@ -1619,30 +1701,65 @@ void server_loop(gs_server *sv) {
             sl.busy = false;
             sv->done_cv.notify_all();
         }
-        // admissions, first come first served, while memory and a slot are free
+        // admissions, first come first served, while memory and a slot are free; queued requests
+        // of the head's scene join its group (dynamic batching, up to batch_views requests)
         while (!sv->queue.empty()) {
-            ServerReq &r = sv->reqs[sv->queue.front()];
-            if (sv->reserved > 0 && sv->reserved + r.bytes > sv->budget) break;
-            int free_slot = -1;
+            ServerReq &head = sv->reqs[sv->queue.front()];
+            if (sv->reserved > 0 && sv->reserved + head.bytes > sv->budget) break;
+            std::vector<size_t> free_slots;
             for (size_t i = 0; i < sv->slots.size(); ++i)
-                if (!sv->slots[i].busy) {
-                    free_slot = (int)i;
-                    break;
+                if (!sv->slots[i].busy) free_slots.push_back(i);
+            if (free_slots.empty()) break;
+            if (sv->batch_wait_ms > 0.0 && free_slots.size() < sv->slots.size()) {
+                // batching window: while more of the head's scene's requests are queued than
+                // slots are free and busy slots will free up, hold admission for up to
+                // batch_wait_ms from when the hold began
+                size_t same = 0;
+                const size_t scan = std::min(sv->queue.size(), (size_t)64);
+                for (size_t q = 0; q < scan; ++q)
+                    if (sv->reqs[sv->queue[q]].model == head.model) ++same;
+                if (free_slots.size() < std::min<size_t>(same, sv->batch_views)) {
+                    const double t = now_ms();
+                    if (sv->hold_since < 0.0) sv->hold_since = t;
+                    if (t - sv->hold_since < sv->batch_wait_ms) {
+                        busy = true;  // poll again soon
+                        break;
+                    }
                 }
-            if (free_slot < 0) break;
-            ServerSlot &sl = sv->slots[free_slot];
-            const uint64_t id = sv->queue.front();
-            sv->queue.pop_front();
-            r.slot = free_slot;
-            r.state = 1;
-            sv->reserved += r.bytes;
-            sl.busy = true;
-            sl.req = id;
-            if (server_launch(sv, r, sl) != GS_OK) {
-                r.state = 3;
-                ++sv->failed;
-                sv->reserved -= r.bytes;
-                sl.busy = false;
+            }
+            sv->hold_since = -1.0;
+            std::vector<std::pair<uint64_t, size_t>> members;  // (request id, slot)
+            size_t reserve = 0;
+            const size_t scan = std::min(sv->queue.size(), (size_t)64);
+            std::vector<size_t> taken;  // queue positions
+            for (size_t q = 0; q < scan && members.size() < free_slots.size() && members.size() < sv->batch_views; ++q) {
+                const uint64_t id = sv->queue[q];
+                ServerReq &r = sv->reqs[id];
+                if (q > 0 && r.model != head.model) continue;
+                if (q > 0 && sv->reserved + reserve + r.bytes > sv->budget) continue;
+                members.emplace_back(id, free_slots[members.size()]);
+                taken.push_back(q);
+                reserve += r.bytes;
+            }
+            for (size_t t = taken.size(); t-- > 0;) sv->queue.erase(sv->queue.begin() + (ptrdiff_t)taken[t]);
+            std::vector<std::pair<ServerReq *, ServerSlot *>> group;
+            for (auto &mb : members) {
+                ServerReq &r = sv->reqs[mb.first];
+                ServerSlot &sl = sv->slots[mb.second];
+                r.slot = (int)mb.second;
+                r.state = 1;
+                sv->reserved += r.bytes;
+                sl.busy = true;
+                sl.req = mb.first;
+                group.emplace_back(&r, &sl);
+            }
+            if (server_launch_group(sv, group) != GS_OK) {
+                for (auto &g : group) {
+                    g.first->state = 3;
+                    ++sv->failed;
+                    sv->reserved -= g.first->bytes;
+                    g.second->busy = false;
+                }
                 sv->done_cv.notify_all();
             } else {
                 busy = true;
@@ -1763,5 +1880,17 @@ gs_status gs_server_reset_stats(gs_server *sv) {
 }
 
 size_t gs_server_request_bytes(uint32_t n, uint32_t width, uint32_t height) { return request_bytes(n, width, height); }
+
+gs_status gs_server_set_batching(gs_server *sv, uint32_t max_views, double max_wait_ms) {
+    if (!sv) return fail(GS_ERR_INVALID_ARG, "server is NULL");
+    if (max_views < 1 || max_views > kPreMaxViews)
+        return fail(GS_ERR_INVALID_ARG, "max_views %u outside 1..%u", max_views, kPreMaxViews);
+    if (!(max_wait_ms >= 0.0 && max_wait_ms <= 1000.0))
+        return fail(GS_ERR_INVALID_ARG, "max_wait_ms %g outside 0..1000", max_wait_ms);
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->batch_views = max_views;
+    sv->batch_wait_ms = max_wait_ms;
+    return GS_OK;
+}
 
 }  // extern "C"

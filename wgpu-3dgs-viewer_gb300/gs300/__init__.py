@@ -491,6 +491,12 @@ class Server:
     def reset_stats(self):
         check(lib().gs_server_reset_stats(self._h))
 
+    def set_batching(self, max_views, max_wait_ms=0.0):
+        """Dynamic batching: up to max_views (1..16) admitted requests of one scene share a
+        preprocess launch (records read once); 1 runs every request alone.  max_wait_ms lets a
+        request wait that long for busy slots to free up so that larger groups form."""
+        check(lib().gs_server_set_batching(self._h, int(max_views), float(max_wait_ms)))
+
     def close(self):
         if getattr(self, "_h", None):
             lib().gs_server_destroy(self._h)

@@ -113,6 +113,7 @@ SIGNATURES = [
     ("gs_server_wait", ST, [P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     ("gs_server_stats", ST, [P, P]),
     ("gs_server_reset_stats", ST, [P]),
+    ("gs_server_set_batching", ST, [P, U32, ctypes.c_double]),
 ]
 
 _lib = None
