@@ -149,3 +149,34 @@ def test_batch_autotune(gs, cuda, monkeypatch):
     mt = gs.model_transform_pod()
     for (w, h), cam, t in zip(plan, cams, targets):
         assert np.array_equal(t.download(), _single(gs, sc, mt, cam, w, h))
+
+
+def test_batching_config_shape(gs, cuda, monkeypatch):
+    """The batching configuration's shape at reduced size: 4 models with random rigid model
+    transforms and 10% of Gaussians carrying a per-Gaussian translation, 16 views of
+    resolutions drawn from {640x360, 1280x720, 1920x1080, 3840x2160} on random orbits of radius
+    6-12, in one batch call; every view equals the Viewer's frame for its model and camera."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    rng = np.random.default_rng(8)
+    sizes = (25_000, 50_000, 75_000, 150_000)
+    scenes, mts = {}, {}
+    for i, n in enumerate(sizes):
+        k = f"m{i}"
+        scenes[k] = S.synth_scene(n, seed=70 + i, translate_fraction=0.1)
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        mts[k] = gs.model_transform_pod(tuple(rng.normal(0.0, 0.5, 3)), tuple(q), (1.0, 1.0, 1.0))
+    mv = gs.MultiModelViewer()
+    for k, sc in scenes.items():
+        mv.insert_model(k, sc)
+        mv.update_model_transform_with_pod(k, mts[k])
+    keys = list(scenes)
+    res = [(640, 360), (1280, 720), (1920, 1080), (3840, 2160)]
+    plan = [(keys[int(rng.integers(0, 4))], res[int(rng.integers(0, 4))]) for _ in range(16)]
+    cams = [S.orbit_camera(int(rng.integers(0, 120)), radius=float(rng.uniform(6, 12))) for _ in plan]
+    targets = [gs.RenderTarget(w, h) for _, (w, h) in plan]
+    batch = gs.Batch(mv, keys)
+    batch.render([(k, gs.CameraPod.new(c, wh), t) for (k, wh), c, t in zip(plan, cams, targets)])
+    batch.synchronize()
+    for (k, (w, h)), cam, t in zip(plan, cams, targets):
+        assert np.array_equal(t.download(), _single(gs, scenes[k], mts[k], cam, w, h))
