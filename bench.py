@@ -529,15 +529,30 @@ def main():
             "traffic": None,
         }
 
-    # ---- end to end through the public API with host buffers ----
-    host = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    # ---- end to end through the public API with host buffers: every frame's camera goes in from
+    # host memory and its pixels come back to pinned host memory inside the timed region; two
+    # targets and host buffers let the host enqueue frame k while frame k-1 is on the GPU ----
+    hosts = [torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True).numpy() for _ in range(2)]
+    targets2 = [target, gs300.RenderTarget(W, H)]
+    copy_stream = torch.cuda.Stream()  # the read-back overlaps the next frame's kernels
+    rendered = [torch.cuda.Event(), torch.cuda.Event()]
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.steps):
+        b = k % 2
+        if k >= 2:
+            stream.wait_event(copied[b])  # target b's previous frame has left the device
         viewer.update_camera_with_pod(pods[k % 120])  # 144-byte CameraPod from host memory
-        viewer.render(target, stream=sh)
-        target.download(host, stream=sh)  # device -> pinned host, synchronises
+        viewer.render(targets2[b], stream=sh)
+        rendered[b].record(stream)
+        copy_stream.wait_event(rendered[b])
+        targets2[b].download_async(hosts[b], stream=copy_stream.cuda_stream)  # device -> pinned host
+        copied[b].record(copy_stream)
+        if k >= 1:
+            copied[1 - b].synchronize()  # frame k-1's pixels are on the host
+    torch.cuda.synchronize()
     e2e_rate, _ = group.job_rate(args.steps, time.perf_counter() - t0)
     e2e = {"value": e2e_rate, "unit": "frames/s", "h2d_bytes_per_step": 144,
            "d2h_bytes_per_step": W * H * 4}

@@ -275,6 +275,9 @@ uint8_t *gs_target_data(gs_target *target);
 uint32_t gs_target_pitch(const gs_target *target);
 /* Copy the target to host memory (width*height*4 bytes, tightly packed) and wait. */
 gs_status gs_target_download(gs_target *target, uint8_t *host_rgba, gs_stream stream);
+/* The same copy enqueued on `stream` without waiting (the bytes are on the host once the stream
+ * reaches it); `host_rgba` should be pinned memory for the copy to overlap other work. */
+gs_status gs_target_download_async(gs_target *target, uint8_t *host_rgba, gs_stream stream);
 
 /* ------------------------------------------------------------------------------------------ */
 /* MultiModelViewer facade (src/multi_model.rs:289-531).                                      */

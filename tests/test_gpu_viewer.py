@@ -202,3 +202,16 @@ def test_viewer_half_records(gs, cuda, oracle, fmt):
     want, *_ = oracle.render(u, sc, fmt, w, h, exp_mode=1, threads=16)
     got = t.download()
     assert within_one_fraction(got, want) >= 0.999 and frame_psnr(got, want) >= 45.0
+
+
+def test_download_async_matches_download(gs, cuda):
+    sc = S.synth_scene(30_000, seed=77)
+    v = gs.Viewer(sc)
+    v.update_camera(S.orbit_camera(5), (320, 180))
+    t = gs.RenderTarget(320, 180)
+    s = cuda.cuda.Stream()
+    v.render(t, stream=s.cuda_stream)
+    pinned = cuda.empty((180, 320, 4), dtype=cuda.uint8, pin_memory=True).numpy()
+    t.download_async(pinned, stream=s.cuda_stream)
+    s.synchronize()
+    assert np.array_equal(pinned, t.download())

@@ -791,6 +791,13 @@ gs_status gs_target_download(gs_target *t, uint8_t *host, gs_stream stream) {
     return GS_OK;
 }
 
+gs_status gs_target_download_async(gs_target *t, uint8_t *host, gs_stream stream) {
+    if (!t || !host) return fail(GS_ERR_INVALID_ARG, "NULL argument");
+    GS_CUDA(cudaMemcpyAsync(host, t->buf.ptr, (size_t)t->w * t->h * 4, cudaMemcpyDeviceToHost,
+                            (cudaStream_t)stream));
+    return GS_OK;
+}
+
 }  // extern "C"
 
 // ---- MultiModelViewer -----------------------------------------------------------------------

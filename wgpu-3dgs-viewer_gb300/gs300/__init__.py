@@ -218,6 +218,12 @@ class RenderTarget:
         check(lib().gs_target_download(self._h, out.ctypes.data_as(ctypes.c_void_p), _stream(stream)))
         return out
 
+    def download_async(self, out, stream=None):
+        """Enqueue the copy into `out` (pinned host memory) on `stream` without waiting."""
+        assert out.flags["C_CONTIGUOUS"] and out.nbytes >= self.width * self.height * 4
+        check(lib().gs_target_download_async(self._h, out.ctypes.data_as(ctypes.c_void_p), _stream(stream)))
+        return out
+
     def close(self):
         if getattr(self, "_h", None):
             lib().gs_target_destroy(self._h)

@@ -84,6 +84,7 @@ SIGNATURES = [
     ("gs_target_data", P, [P]),
     ("gs_target_pitch", U32, [P]),
     ("gs_target_download", ST, [P, P, P]),
+    ("gs_target_download_async", ST, [P, P, P]),
     ("gs_multi_viewer_create", ST, [PP]),
     ("gs_multi_viewer_destroy", None, [P]),
     ("gs_multi_viewer_insert_model", ST, [P, CP, P, U32, U32]),
