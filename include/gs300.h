@@ -352,6 +352,8 @@ typedef struct gs_tuning {
     uint32_t streams;          /* streams the captured graph fans out over, 1..16 */
     uint32_t sort_match;       /* depth sort ranking: 1 = match.any, 0 = one ballot per digit bit */
     uint32_t hist_blocks;      /* depth sort key-histogram blocks, 0 (by key count) or 1..1216 */
+    uint32_t raster_grid;      /* 0: each view rasterised after its own binning (overlapping other
+                                  views' sorting); 1: one rasteriser grid over all views' tiles */
 } gs_tuning;
 /* The library's defaults (GS300_SUFFIX_MIN / GS300_SUFFIX_EPS override the raster knobs). */
 gs_status gs_tuning_default(gs_tuning *out);

@@ -97,10 +97,13 @@ TUNINGS = [
     dict(views_per_launch=1, streams=1),
     dict(suffix_min=1, eps=0.3),            # every tile takes the early-out, with frequent restarts
     dict(sort_match=0, hist_blocks=7, views_per_launch=3, streams=5),
+    dict(raster_grid=1),                    # one rasteriser grid over all views
+    dict(raster_grid=1, views_per_launch=2, streams=3, suffix_min=1),
 ]
 
 
-@pytest.mark.parametrize("knobs", TUNINGS, ids=["serial", "early_out_everywhere", "ballot_sort"])
+@pytest.mark.parametrize("knobs", TUNINGS, ids=["serial", "early_out_everywhere", "ballot_sort", "one_grid",
+                                                "one_grid_early_out"])
 def test_batch_tuning_changes_no_frame(gs, cuda, monkeypatch, knobs):
     monkeypatch.setenv("GS300_EXACT_EXP", "1")
     sc = S.synth_scene(40_000, seed=12)
@@ -124,7 +127,8 @@ def test_batch_tuning_rejects_bad_values(gs, cuda):
     mv.insert_model("m", S.synth_scene(100, seed=1))
     batch = gs.Batch(mv, ["m"])
     for bad in (dict(views_per_launch=0), dict(views_per_launch=17), dict(streams=0), dict(streams=17),
-                dict(sort_match=2), dict(eps=0.0), dict(eps=0.7), dict(suffix_min=0), dict(hist_blocks=5000)):
+                dict(sort_match=2), dict(eps=0.0), dict(eps=0.7), dict(suffix_min=0), dict(hist_blocks=5000),
+                dict(raster_grid=2)):
         with pytest.raises(gs.GsError):
             batch.set_tuning(**bad)
     assert batch.tuning == gs.tuning_default()
@@ -176,7 +180,37 @@ def test_batching_config_shape(gs, cuda, monkeypatch):
     cams = [S.orbit_camera(int(rng.integers(0, 120)), radius=float(rng.uniform(6, 12))) for _ in plan]
     targets = [gs.RenderTarget(w, h) for _, (w, h) in plan]
     batch = gs.Batch(mv, keys)
-    batch.render([(k, gs.CameraPod.new(c, wh), t) for (k, wh), c, t in zip(plan, cams, targets)])
-    batch.synchronize()
-    for (k, (w, h)), cam, t in zip(plan, cams, targets):
-        assert np.array_equal(t.download(), _single(gs, scenes[k], mts[k], cam, w, h))
+    want = [_single(gs, scenes[k], mts[k], cam, w, h) for (k, (w, h)), cam in zip(plan, cams)]
+    for grid in (0, 1):  # views rasterised one by one, then one grid over all views' tiles
+        batch.set_tuning(raster_grid=grid)
+        batch.render([(k, gs.CameraPod.new(c, wh), t) for (k, wh), c, t in zip(plan, cams, targets)])
+        batch.synchronize()
+        for t, w_ in zip(targets, want):
+            assert np.array_equal(t.download(), w_)
+
+
+def test_batch_renders_back_to_back(gs, cuda, monkeypatch):
+    """Two batch renders with different cameras enqueued without a sync between them (each read
+    back asynchronously): each read-back holds its own cameras' frames."""
+    monkeypatch.setenv("GS300_EXACT_EXP", "1")
+    sc = S.synth_scene(40_000, seed=14)
+    mv = gs.MultiModelViewer()
+    mv.insert_model("m", sc)
+    batch = gs.Batch(mv, ["m"])
+    plan = [(320, 180), (256, 144), (400, 200)]
+    targets = [gs.RenderTarget(w, h) for w, h in plan]
+    s = cuda.cuda.Stream()
+    rounds = []
+    for r in range(3):
+        cams = [S.orbit_camera(20 * r + 3 * j, radius=6.0) for j in range(len(plan))]
+        batch.render([("m", gs.CameraPod.new(c, wh), t) for wh, c, t in zip(plan, cams, targets)], stream=s.cuda_stream)
+        hosts = [cuda.empty((h, w, 4), dtype=cuda.uint8, pin_memory=True).numpy() for w, h in plan]
+        for t, hbuf in zip(targets, hosts):
+            t.download_async(hbuf, stream=s.cuda_stream)
+        rounds.append((cams, hosts))
+    s.synchronize()
+    batch.synchronize(stream=s.cuda_stream)
+    mt = gs.model_transform_pod()
+    for cams, hosts in rounds:
+        for (w, h), cam, hbuf in zip(plan, cams, hosts):
+            assert np.array_equal(hbuf, _single(gs, sc, mt, cam, w, h))

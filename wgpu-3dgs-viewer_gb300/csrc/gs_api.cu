@@ -1062,13 +1062,18 @@ struct gs_batch {
     std::vector<std::string> keys;
     std::vector<ViewSlot> slots;
     DevBuf uniforms_dev;
-    gs_frame_uniforms *uniforms_host = nullptr;  // pinned, one per view
-    uint32_t uniforms_cap = 0;
+    // Pinned staging of the views' uniforms: a ring of kUniformRing arrays of uniforms_cap, each
+    // reused only after the copy that read it (event) has run, so renders issued back to back
+    // never upload another render's cameras.
+    gs_frame_uniforms *uniforms_host = nullptr;
+    uint32_t uniforms_cap = 0, uniforms_ring = 0;
+    cudaEvent_t uniforms_copied[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaStream_t> streams;
     std::vector<cudaEvent_t> events;
     std::vector<cudaEvent_t> chunk_events;  // one per multi-view preprocess launch
     DevBuf views_dev;                       // PreView per view (device), rebuilt with the graph
     DevBuf group_dev;                       // one control block per multi-view launch
+    DevBuf jobs_dev, tile_base_dev;         // per view RasterJob and the prefix of tile counts
     uint32_t chunks = 0;
     gs::Tuning tuning = gs::default_tuning();
     cudaStream_t capture = nullptr;
@@ -1083,6 +1088,8 @@ struct gs_batch {
         for (auto s : streams) cudaStreamDestroy(s);
         for (auto e : events) cudaEventDestroy(e);
         for (auto e : chunk_events) cudaEventDestroy(e);
+        for (auto e : uniforms_copied)
+            if (e) cudaEventDestroy(e);
         if (capture) cudaStreamDestroy(capture);
         if (uniforms_host) cudaFreeHost(uniforms_host);
     }
@@ -1105,24 +1112,35 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
         const gs_status s = check_target(views[i].target, views[i].width, views[i].height, views[i].pitch);
         if (s != GS_OK) return s;
     }
-    if (n > b->uniforms_cap) {
-        if (b->uniforms_host) cudaFreeHost(b->uniforms_host);
-        b->uniforms_host = nullptr;
-        GS_CUDA(cudaMallocHost(&b->uniforms_host, (size_t)n * sizeof(gs_frame_uniforms)));
-        GS_CUDA(b->uniforms_dev.ensure((size_t)n * sizeof(gs_frame_uniforms)));
-        b->uniforms_cap = n;
-    }
-    if (b->slots.size() < n) b->slots.resize(n);
-    bool changed = false;
     std::string shape(reinterpret_cast<const char *>(&mv->frame.gt), sizeof(gs_gaussian_transform_pod));
     for (uint32_t i = 0; i < n; ++i) {
-        GS_CUDA(b->slots[i].prepare(ms[i], views[i].width, views[i].height, &changed));
-        const gs_status s = gs_frame_uniforms_build(&views[i].camera, &ms[i]->model, &mv->frame.gt, views[i].width,
-                                                    views[i].height, &b->uniforms_host[i]);
-        if (s != GS_OK) return s;
         const uintptr_t key[7] = {(uintptr_t)ms[i], ms[i]->n, views[i].width, views[i].height, views[i].pitch,
                                   (uintptr_t)views[i].target, (uintptr_t)ms[i]->has_selection};
         shape.append(reinterpret_cast<const char *>(key), sizeof(key));
+    }
+    // A new shape rewrites buffers and descriptor arrays that an earlier render of this batch may
+    // still be reading on the caller's stream: let the device drain first (shape changes are rare).
+    if (shape != b->shape || !b->exec || n > b->uniforms_cap) GS_CUDA(cudaDeviceSynchronize());
+    if (n > b->uniforms_cap) {
+        if (b->uniforms_host) cudaFreeHost(b->uniforms_host);
+        b->uniforms_host = nullptr;
+        GS_CUDA(cudaMallocHost(&b->uniforms_host, (size_t)4 * n * sizeof(gs_frame_uniforms)));
+        GS_CUDA(b->uniforms_dev.ensure((size_t)n * sizeof(gs_frame_uniforms)));
+        b->uniforms_cap = n;
+    }
+    for (auto &e : b->uniforms_copied)
+        if (!e) GS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    const uint32_t ring = b->uniforms_ring;
+    b->uniforms_ring = (ring + 1) % 4;
+    GS_CUDA(cudaEventSynchronize(b->uniforms_copied[ring]));  // its previous copy has run
+    gs_frame_uniforms *uh = b->uniforms_host + (size_t)ring * b->uniforms_cap;
+    if (b->slots.size() < n) b->slots.resize(n);
+    bool changed = false;
+    for (uint32_t i = 0; i < n; ++i) {
+        GS_CUDA(b->slots[i].prepare(ms[i], views[i].width, views[i].height, &changed));
+        const gs_status s = gs_frame_uniforms_build(&views[i].camera, &ms[i]->model, &mv->frame.gt, views[i].width,
+                                                    views[i].height, &uh[i]);
+        if (s != GS_OK) return s;
     }
     if (changed || shape != b->shape || !b->exec) {
         if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -1187,6 +1205,22 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
         }
         b->chunks = (uint32_t)chunks.size();
         const PreView *pv_dev = reinterpret_cast<const PreView *>(b->views_dev.ptr);
+        // One rasteriser grid over every view's tiles: the views' raster jobs (pointers into
+        // their scratch) and the prefix of their tile counts, known before any launch.
+        std::vector<RasterJob> jobs(n);
+        std::vector<uint32_t> tile_base(n + 1, 0u);
+        for (uint32_t i = 0; i < n; ++i) {
+            ViewSlot &v = b->slots[i];
+            uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+            const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, ms[i]->n};
+            jobs[i] = raster_job(&seg, 1, views[i].target, views[i].width, views[i].height, views[i].pitch, v.max_pairs,
+                                 v.raster_scratch.ptr);
+            tile_base[i + 1] = tile_base[i] + jobs[i].ntiles;
+        }
+        GS_CUDA(b->jobs_dev.ensure((size_t)n * sizeof(RasterJob)));
+        GS_CUDA(cudaMemcpy(b->jobs_dev.ptr, jobs.data(), (size_t)n * sizeof(RasterJob), cudaMemcpyHostToDevice));
+        GS_CUDA(b->tile_base_dev.ensure((size_t)(n + 1) * 4));
+        GS_CUDA(cudaMemcpy(b->tile_base_dev.ptr, tile_base.data(), (size_t)(n + 1) * 4, cudaMemcpyHostToDevice));
         GS_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
         t_capturing = true;
         t_captured_launches = 0;
@@ -1213,9 +1247,13 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
                 if (err == cudaSuccess) {
                     const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1,
                                             ms[i]->n};
-                    err = launch_raster(&seg, 1, b->uniforms_host[i], views[i].target, views[i].width,
-                                        views[i].height, views[i].pitch, v.max_pairs, v.raster_scratch.ptr,
-                                        mv->frame.exact_exp, vs, &b->tuning);
+                    if (b->tuning.raster_grid)
+                        err = launch_binning(&seg, 1, uh[i], views[i].width, views[i].height, v.max_pairs,
+                                             v.raster_scratch.ptr, vs);
+                    else
+                        err = launch_raster(&seg, 1, uh[i], views[i].target, views[i].width, views[i].height,
+                                            views[i].pitch, v.max_pairs, v.raster_scratch.ptr, mv->frame.exact_exp, vs,
+                                            &b->tuning);
                 }
             }
         }
@@ -1223,6 +1261,10 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
             err = cudaEventRecord(b->events[s], b->streams[s]);
             if (err == cudaSuccess) err = cudaStreamWaitEvent(b->capture, b->events[s], 0);
         }
+        if (err == cudaSuccess && b->tuning.raster_grid)
+            err = launch_raster_views(reinterpret_cast<const RasterJob *>(b->jobs_dev.ptr),
+                                      reinterpret_cast<const uint32_t *>(b->tile_base_dev.ptr), n, tile_base[n],
+                                      uh[0], mv->frame.exact_exp, b->capture, &b->tuning);
         t_capturing = false;
         cudaGraph_t graph = nullptr;
         const cudaError_t end = cudaStreamEndCapture(b->capture, &graph);
@@ -1233,8 +1275,9 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
         b->graph_launches = t_captured_launches;
         b->shape = shape;
     }
-    GS_CUDA(cudaMemcpyAsync(b->uniforms_dev.ptr, b->uniforms_host, (size_t)n * sizeof(gs_frame_uniforms),
-                            cudaMemcpyHostToDevice, st));
+    GS_CUDA(cudaMemcpyAsync(b->uniforms_dev.ptr, uh, (size_t)n * sizeof(gs_frame_uniforms), cudaMemcpyHostToDevice,
+                            st));
+    GS_CUDA(cudaEventRecord(b->uniforms_copied[ring], st));
     GS_CUDA(cudaGraphLaunch(b->exec, st));
     gs::g_launches.fetch_add(b->graph_launches, std::memory_order_relaxed);
     b->last.assign(views, views + n);
@@ -1321,6 +1364,7 @@ gs_tuning to_public(const gs::Tuning &t) {
     o.streams = t.streams;
     o.sort_match = t.sort_match;
     o.hist_blocks = t.hist_blocks;
+    o.raster_grid = t.raster_grid;
     return o;
 }
 
@@ -1334,12 +1378,14 @@ gs_status from_public(const gs_tuning *p, gs::Tuning *t) {
         return fail(GS_ERR_INVALID_ARG, "streams %u outside 1..%u", p->streams, kBatchStreams);
     if (p->sort_match > 1) return fail(GS_ERR_INVALID_ARG, "sort_match must be 0 or 1");
     if (p->hist_blocks > 152 * 8) return fail(GS_ERR_INVALID_ARG, "hist_blocks %u above 1216", p->hist_blocks);
+    if (p->raster_grid > 1) return fail(GS_ERR_INVALID_ARG, "raster_grid must be 0 or 1");
     t->suffix_min = p->suffix_min;
     t->eps = p->eps;
     t->views_per_launch = p->views_per_launch;
     t->streams = p->streams;
     t->sort_match = p->sort_match;
     t->hist_blocks = p->hist_blocks;
+    t->raster_grid = p->raster_grid;
     return GS_OK;
 }
 
@@ -1435,9 +1481,16 @@ gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n,
     const uint32_t streams_c[] = {4, 8, 16};
     const uint32_t match_c[] = {0, 1};
     const uint32_t hist_c[] = {0, 304, 608};
+    const uint32_t grid_c[] = {0, 1};
     for (uint32_t round = 0; round < rounds && s == GS_OK; ++round) {
-        for (int knob = 0; knob < 6 && s == GS_OK; ++knob) {
-            const size_t nc = knob == 0 ? 4 : knob == 1 ? 2 : knob == 2 ? 4 : knob == 3 ? 3 : knob == 4 ? 2 : 3;
+        for (int knob = 0; knob < 7 && s == GS_OK; ++knob) {
+            const size_t nc = knob == 0   ? 4
+                              : knob == 1 ? 2
+                              : knob == 2 ? 4
+                              : knob == 3 ? 3
+                              : knob == 4 ? 2
+                              : knob == 5 ? 3
+                                          : 2;
             for (size_t c = 0; c < nc && s == GS_OK; ++c) {
                 gs::Tuning t = best;
                 switch (knob) {
@@ -1446,10 +1499,12 @@ gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n,
                     case 2: t.views_per_launch = vpl_c[c]; break;
                     case 3: t.streams = streams_c[c]; break;
                     case 4: t.sort_match = match_c[c]; break;
-                    default: t.hist_blocks = hist_c[c]; break;
+                    case 5: t.hist_blocks = hist_c[c]; break;
+                    default: t.raster_grid = grid_c[c]; break;
                 }
                 if (t.suffix_min == best.suffix_min && t.eps == best.eps && t.views_per_launch == best.views_per_launch &&
-                    t.streams == best.streams && t.sort_match == best.sort_match && t.hist_blocks == best.hist_blocks)
+                    t.streams == best.streams && t.sort_match == best.sort_match && t.hist_blocks == best.hist_blocks &&
+                    t.raster_grid == best.raster_grid)
                     continue;
                 double ms = 0.0;
                 s = measure(t, &ms);

@@ -72,6 +72,8 @@ struct Tuning {
     uint32_t streams = 16;          // batch: streams the captured graph fans out over (1..16)
     uint32_t sort_match = 1;        // depth sort: 1 = match.any ranking, 0 = a ballot per digit bit
     uint32_t hist_blocks = 0;       // depth sort: key-histogram grid (0 = by key count, <= 1216)
+    uint32_t raster_grid = 0;       // batch: 0 = each view rasterised after its own binning,
+                                    // 1 = one rasteriser grid over all views after all binning
 };
 // The defaults, with GS300_SUFFIX_MIN / GS300_SUFFIX_EPS / GS300_HIST_BLOCKS overriding them.
 Tuning default_tuning();
@@ -112,5 +114,28 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
                           const Tuning *tuning = nullptr);
 // Scratch control block of a raster call (status, pair counts).
 const Ctrl *raster_ctrl(const void *scratch);
+
+// What the rasteriser needs of one view after binning: its splats, tile-sorted pairs, tile
+// ranges, target and status block.  Pure pointer arithmetic on the view's raster scratch, so it
+// can be known (and uploaded for a multi-view grid) before any launch.
+struct RasterJob {
+    const gs_splat *splats;
+    const uint2 *pairs;
+    const uint2 *ranges;
+    uint8_t *target;
+    uint32_t W, H, pitch, tiles_x, max_splats, ntiles;
+    Ctrl *ctrl;
+};
+RasterJob raster_job(const RasterSegment *segs, uint32_t nseg, uint8_t *target, uint32_t width, uint32_t height,
+                     uint32_t pitch, uint32_t max_pairs, void *scratch);
+// Binning, tile sort and tile ranges of one view (everything launch_raster does before the
+// rasteriser itself).
+cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint32_t width,
+                           uint32_t height, uint32_t max_pairs, void *scratch, cudaStream_t st);
+// One rasteriser grid over several binned views (same display mode and std): tile_base holds the
+// prefix of the views' tile counts (nviews + 1 entries, device), jobs the views (device).
+cudaError_t launch_raster_views(const RasterJob *jobs, const uint32_t *tile_base, uint32_t nviews,
+                                uint32_t total_tiles, const gs_frame_uniforms &u, int exact_exp, cudaStream_t st,
+                                const Tuning *tuning = nullptr);
 
 }  // namespace gs

@@ -606,18 +606,17 @@ __device__ __forceinline__ uint32_t compact_chunk(RasterShared &S, uint32_t cnt,
 //      value, which is exact).
 // Every pixel therefore ends bit-identical to the full back-to-front pass.
 template <uint32_t MODE, bool PORTABLE_EXP, bool COUNT>
-__global__ void __launch_bounds__(kRasterThreads) raster_kernel(
-    const gs_splat *__restrict__ sorted, const uint2 *__restrict__ pairs, const uint2 *__restrict__ ranges,
-    uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch, uint32_t tiles_x, float std2,
-    float outline2, uint32_t max_splats, uint32_t suffix_min, float eps, unsigned long long *counters,
-    Ctrl *pctrl) {
-    __shared__ RasterShared S;
+__device__ __forceinline__ void raster_tile(
+    RasterShared &S, const gs_splat *__restrict__ sorted, const uint2 *__restrict__ pairs,
+    const uint2 *__restrict__ ranges, uint8_t *__restrict__ target, uint32_t W, uint32_t H, uint32_t pitch,
+    uint32_t tiles_x, float std2, float outline2, uint32_t max_splats, uint32_t suffix_min, float eps,
+    unsigned long long *counters, Ctrl *pctrl, uint32_t tile) {
     // Work tallies of the counting variant (profiling only): fragment evaluations, alphas,
     // channel-triple blends and transmittance updates.
     uint32_t n_eval = 0, n_alpha = 0, n_blend = 0, n_trans = 0;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-    const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
-    uint2 range = ranges[blockIdx.x];
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+    uint2 range = ranges[tile];
     if (range.y < range.x || range.y > pctrl->count) {
         if (threadIdx.x == 0) atomicOr(&pctrl->status, kStatusBounds);
         range = make_uint2(0u, 0u);
@@ -778,6 +777,37 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(
     }
 }
 
+
+template <uint32_t MODE, bool PORTABLE_EXP, bool COUNT>
+__global__ void __launch_bounds__(kRasterThreads) raster_kernel(const RasterJob J, float std2, float outline2,
+                                                                uint32_t suffix_min, float eps,
+                                                                unsigned long long *counters) {
+    __shared__ RasterShared S;
+    raster_tile<MODE, PORTABLE_EXP, COUNT>(S, J.splats, J.pairs, J.ranges, J.target, J.W, J.H, J.pitch, J.tiles_x,
+                                           std2, outline2, J.max_splats, suffix_min, eps, counters, J.ctrl,
+                                           blockIdx.x);
+}
+
+// One grid over the tiles of several views (a batch): CTA b rasterises tile b - tile_base[v] of
+// the view v with tile_base[v] <= b < tile_base[v + 1].
+template <uint32_t MODE, bool PORTABLE_EXP>
+__global__ void __launch_bounds__(kRasterThreads, 6) raster_views_kernel(const RasterJob *__restrict__ jobs,
+                                                                      const uint32_t *__restrict__ tile_base,
+                                                                      uint32_t nviews, float std2, float outline2,
+                                                                      uint32_t suffix_min, float eps) {
+    __shared__ RasterShared S;
+    uint32_t lo = 0, hi = nviews - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (tile_base[mid] <= blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const RasterJob &J = jobs[lo];
+    raster_tile<MODE, PORTABLE_EXP, false>(S, J.splats, J.pairs, J.ranges, J.target, J.W, J.H, J.pitch, J.tiles_x,
+                                           std2, outline2, J.max_splats, suffix_min, eps, nullptr, J.ctrl,
+                                           blockIdx.x - tile_base[lo]);
+}
+
 // Work tallies of the counting raster variant (profiling only).
 static __device__ unsigned long long g_raster_counts[4];
 
@@ -791,30 +821,85 @@ cudaError_t raster_counters(unsigned long long out[4], bool reset) {
 }
 
 template <uint32_t MODE>
-static void launch_raster_mode(const RasterLayout &L, const gs_splat *splats, uint8_t *target, uint32_t W, uint32_t H,
-                               uint32_t pitch, float std2, float outline2, int exact, uint32_t max_splats,
+static void launch_raster_mode(const RasterJob &J, uint32_t ntiles, float std2, float outline2, int exact,
                                cudaStream_t st, const Tuning &t) {
     if (exact) {
-        raster_kernel<MODE, true, false><<<L.ntiles, kRasterThreads, 0, st>>>(
-            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
-            nullptr, L.ctrl);
+        raster_kernel<MODE, true, false><<<ntiles, kRasterThreads, 0, st>>>(J, std2, outline2, t.suffix_min, t.eps,
+                                                                            nullptr);
     } else if (MODE == GS_DISPLAY_SPLAT && prof_enabled()) {
         unsigned long long *counts = nullptr;
         cudaGetSymbolAddress((void **)&counts, g_raster_counts);
-        raster_kernel<GS_DISPLAY_SPLAT, false, true><<<L.ntiles, kRasterThreads, 0, st>>>(
-            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
-            counts, L.ctrl);
+        raster_kernel<GS_DISPLAY_SPLAT, false, true><<<ntiles, kRasterThreads, 0, st>>>(J, std2, outline2,
+                                                                                       t.suffix_min, t.eps, counts);
     } else {
-        raster_kernel<MODE, false, false><<<L.ntiles, kRasterThreads, 0, st>>>(
-            splats, L.pairs, L.ranges, target, W, H, pitch, L.tiles_x, std2, outline2, max_splats, t.suffix_min, t.eps,
-            nullptr, L.ctrl);
+        raster_kernel<MODE, false, false><<<ntiles, kRasterThreads, 0, st>>>(J, std2, outline2, t.suffix_min, t.eps,
+                                                                             nullptr);
     }
 }
 
-cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
-                          uint32_t W, uint32_t H, uint32_t pitch, uint32_t max_pairs, void *scratch, int exact_exp,
-                          cudaStream_t st, const Tuning *tuning) {
+template <uint32_t MODE>
+static void launch_raster_views_mode(const RasterJob *jobs, const uint32_t *tile_base, uint32_t nviews,
+                                     uint32_t total_tiles, float std2, float outline2, int exact, cudaStream_t st,
+                                     const Tuning &t) {
+    if (exact)
+        raster_views_kernel<MODE, true><<<total_tiles, kRasterThreads, 0, st>>>(jobs, tile_base, nviews, std2,
+                                                                                 outline2, t.suffix_min, t.eps);
+    else
+        raster_views_kernel<MODE, false><<<total_tiles, kRasterThreads, 0, st>>>(jobs, tile_base, nviews, std2,
+                                                                                  outline2, t.suffix_min, t.eps);
+}
+
+RasterJob raster_job(const RasterSegment *segs, uint32_t nseg, uint8_t *target, uint32_t W, uint32_t H,
+                     uint32_t pitch, uint32_t max_pairs, void *scratch) {
+    uint32_t max_splats = 0;
+    for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
+    const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
+    RasterJob J;
+    // Pair values index the model's own splat array (one segment) or the draw-ordered copy.
+    J.splats = nseg == 1 ? segs[0].splats : L.sorted;
+    J.max_splats = nseg == 1 ? segs[0].max_count : max_splats;
+    J.pairs = L.pairs;
+    J.ranges = L.ranges;
+    J.target = target;
+    J.W = W;
+    J.H = H;
+    J.pitch = pitch;
+    J.tiles_x = L.tiles_x;
+    J.ntiles = L.ntiles;
+    J.ctrl = L.ctrl;
+    return J;
+}
+
+cudaError_t launch_raster_views(const RasterJob *jobs_dev, const uint32_t *tile_base_dev, uint32_t nviews,
+                                uint32_t total_tiles, const gs_frame_uniforms &u, int exact_exp, cudaStream_t st,
+                                const Tuning *tuning) {
+    if (nviews == 0 || total_tiles == 0) return cudaSuccess;
     const Tuning tn = tuning ? *tuning : default_tuning();
+    const float std2 = u.std_dev * u.std_dev;
+    const float o = u.std_dev - 0.1f;
+    const float outline2 = o * o;
+    prof_mark(kProfRaster, true, st);
+    count_launches(1);
+    switch (u.display_mode) {
+        case GS_DISPLAY_SPLAT:
+            launch_raster_views_mode<GS_DISPLAY_SPLAT>(jobs_dev, tile_base_dev, nviews, total_tiles, std2, outline2,
+                                                       exact_exp, st, tn);
+            break;
+        case GS_DISPLAY_ELLIPSE:
+            launch_raster_views_mode<GS_DISPLAY_ELLIPSE>(jobs_dev, tile_base_dev, nviews, total_tiles, std2, outline2,
+                                                         exact_exp, st, tn);
+            break;
+        default:
+            launch_raster_views_mode<GS_DISPLAY_POINT>(jobs_dev, tile_base_dev, nviews, total_tiles, std2, outline2,
+                                                       exact_exp, st, tn);
+            break;
+    }
+    prof_mark(kProfRaster, false, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint32_t W,
+                           uint32_t H, uint32_t max_pairs, void *scratch, cudaStream_t st) {
     uint32_t max_splats = 0;
     for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
     const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
@@ -884,23 +969,31 @@ cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_fra
         prof_mark(kProfRanges, false, st);
         count_launches(1);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
+                          uint32_t W, uint32_t H, uint32_t pitch, uint32_t max_pairs, void *scratch, int exact_exp,
+                          cudaStream_t st, const Tuning *tuning) {
+    const Tuning tn = tuning ? *tuning : default_tuning();
+    cudaError_t e = launch_binning(segs, nseg, u, W, H, max_pairs, scratch, st);
+    if (e != cudaSuccess) return e;
+    const RasterJob J = raster_job(segs, nseg, target, W, H, pitch, max_pairs, scratch);
+    if (J.ntiles == 0) return cudaSuccess;
     const float std2 = u.std_dev * u.std_dev;
     const float o = u.std_dev - 0.1f;
     const float outline2 = o * o;
-    // Pair values index the model's own splat array (one segment) or the draw-ordered copy.
-    const gs_splat *rsplats = nseg == 1 ? segs[0].splats : L.sorted;
-    const uint32_t rmax = nseg == 1 ? segs[0].max_count : max_splats;
     prof_mark(kProfRaster, true, st);
     count_launches(1);
     switch (u.display_mode) {
         case GS_DISPLAY_SPLAT:
-            launch_raster_mode<GS_DISPLAY_SPLAT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st, tn);
+            launch_raster_mode<GS_DISPLAY_SPLAT>(J, J.ntiles, std2, outline2, exact_exp, st, tn);
             break;
         case GS_DISPLAY_ELLIPSE:
-            launch_raster_mode<GS_DISPLAY_ELLIPSE>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st, tn);
+            launch_raster_mode<GS_DISPLAY_ELLIPSE>(J, J.ntiles, std2, outline2, exact_exp, st, tn);
             break;
         default:
-            launch_raster_mode<GS_DISPLAY_POINT>(L, rsplats, target, W, H, pitch, std2, outline2, exact_exp, rmax, st, tn);
+            launch_raster_mode<GS_DISPLAY_POINT>(J, J.ntiles, std2, outline2, exact_exp, st, tn);
             break;
     }
     prof_mark(kProfRaster, false, st);

@@ -185,6 +185,7 @@ class Tuning(ctypes.Structure):
         ("streams", ctypes.c_uint32),
         ("sort_match", ctypes.c_uint32),
         ("hist_blocks", ctypes.c_uint32),
+        ("raster_grid", ctypes.c_uint32),
     ]
 
     def as_dict(self):
