@@ -176,11 +176,21 @@ float exp_portable(float x) {
     return p * scale;
 }
 
-// Upper bound on r² beyond which a splat fragment cannot change an 8-bit destination:
-// alpha·exp(-r²) <= 1/512 whenever r² >= ln(512·alpha); ln(x) <= ln2·(e + (m - 1) + 0.0861)
-// for x = m·2^e, m in [1, 2).  Used only to size the pixel box of a splat.
-float splat_r2_bound(float alpha, float std2) {
-    const float x = 512.0f * alpha;
+// Upper bound on r² beyond which a splat fragment cannot change an 8-bit destination (sizes the
+// pixel box of a splat).  A fragment of alpha a moves a channel of destination d in [0, 255] by
+// a·(s - d), |s - d| <= reach = max over the channels of max(s, 255 - s); a·reach <= 0.499 keeps
+// the rounded result at d.  a = alpha·exp(-r²) <= 0.499/reach whenever r² >= ln(alpha·reach/0.499);
+// ln(x) <= ln2·(e + (m - 1) + 0.0861) for x = m·2^e, m in [1, 2).
+float colour_reach(float s0, float s1, float s2) {
+    const float t0 = s0 > 255.0f - s0 ? s0 : 255.0f - s0;
+    const float t1 = s1 > 255.0f - s1 ? s1 : 255.0f - s1;
+    const float t2 = s2 > 255.0f - s2 ? s2 : 255.0f - s2;
+    const float t01 = t0 > t1 ? t0 : t1;
+    return t01 > t2 ? t01 : t2;
+}
+
+float splat_r2_bound(float alpha, float reach, float std2) {
+    const float x = (alpha * reach) * 2.0041f;
     if (!(x > 0.0f)) return -1.0f;
     const uint32_t bits = f2u(x);
     const float e = (float)((int)((bits >> 23) & 0xFFu) - 127);
@@ -425,7 +435,8 @@ Pre preprocess_one(const gs_frame_uniforms &u, const Record &g, gs_splat *splat)
     splat->q[1] = -a01 / det;
     splat->q[2] = -a10 / det;
     splat->q[3] = a00 / det;
-    const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
+    const float reach = colour_reach(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f);
+    const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], reach, std2) : std2;
     const bool ok = det != 0.0f && std::isfinite(det) && std::isfinite(splat->q[0]) &&
                     std::isfinite(splat->q[1]) && std::isfinite(splat->q[2]) &&
                     std::isfinite(splat->q[3]) && r2 >= 0.0f;

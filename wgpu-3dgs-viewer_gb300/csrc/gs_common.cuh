@@ -183,10 +183,21 @@ __device__ __forceinline__ float exp_portable(float x) {
     return __fmul_rn(p, __uint_as_float((uint32_t)(ki + 127) << 23));
 }
 
-// Fragment-bearing r² bound of a splat (see gs_splat.ex): a fragment with
-// alpha·exp(-r²) <= 1/512 cannot move an 8-bit channel; ln x <= ln2·(e + m - 1 + 0.0861).
-__device__ __forceinline__ float splat_r2_bound(float alpha, float std2) {
-    const float x = 512.0f * alpha;
+// Fragment-bearing r² bound of a splat (see gs_splat.ex).  A fragment of alpha a moves a channel
+// of destination d in [0, 255] by a·(s - d), |s - d| <= m = max over the colour channels of
+// max(s, 255 - s); with a·m <= 0.499 (plus FP32 rounding far below 1e-3) the rounded blend gives
+// d back, so the fragment cannot change the pixel.  a = alpha·exp(-r²) <= 0.499/m whenever
+// r² >= ln(alpha·m/0.499); ln x <= ln2·(e + mant - 1 + 0.0861) for x = mant·2^e, plus margins.
+__host__ __device__ __forceinline__ float splat_colour_reach(float s0, float s1, float s2) {
+    const float t0 = s0 > 255.0f - s0 ? s0 : 255.0f - s0;
+    const float t1 = s1 > 255.0f - s1 ? s1 : 255.0f - s1;
+    const float t2 = s2 > 255.0f - s2 ? s2 : 255.0f - s2;
+    const float t01 = t0 > t1 ? t0 : t1;
+    return t01 > t2 ? t01 : t2;
+}
+
+__device__ __forceinline__ float splat_r2_bound(float alpha, float reach, float std2) {
+    const float x = (alpha * reach) * 2.0041f;  // >= alpha·reach / 0.499
     if (!(x > 0.0f)) return -1.0f;
     const uint32_t bits = __float_as_uint(x);
     const float e = (float)((int)((bits >> 23) & 0xFFu) - 127);

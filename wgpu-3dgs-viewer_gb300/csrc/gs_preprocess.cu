@@ -392,7 +392,9 @@ __device__ __forceinline__ void write_splat(const gs_frame_uniforms &u, const Re
         q1 = -a01 / det;
         q2 = -a10 / det;
         q3 = a00 / det;
-        const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], std2) : std2;
+        const float reach = splat_colour_reach(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f,
+                                               clamp01(rgba[2]) * 255.0f);
+        const float r2 = (u.display_mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(rgba[3], reach, std2) : std2;
         const bool ok = det != 0.0f && isfinite(det) && isfinite(q0) && isfinite(q1) && isfinite(q2) &&
                         isfinite(q3) && r2 >= 0.0f;
         if (ok) {

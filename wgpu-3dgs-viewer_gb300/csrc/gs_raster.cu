@@ -13,7 +13,7 @@
 //     it evaluates the interpolated quad offset q, the discard test, the alpha of the display
 //     mode, and blends with the 8-bit re-quantisation a Rgba8Unorm attachment performs after
 //     every fragment: d' = round(d·(1-α) + s·α) in units of 1/255.
-// Fragments whose alpha cannot move an 8-bit channel (alpha <= 1/512) lie outside the splat's
+// Fragments whose alpha cannot move an 8-bit channel (see splat_r2_bound) lie outside the splat's
 // fragment box and are never visited; skipping them leaves every pixel bit-identical.
 #include <cstdlib>
 
@@ -205,7 +205,9 @@ __global__ void __launch_bounds__(kBinThreads) bin_count_kernel(
             // The footprint is convex and its box meets every tile of the rectangle, so only the
             // corner tiles of a rectangle (up to 16 tiles) can miss it; drop those that do.
             if (mode != GS_DISPLAY_POINT && cnt > 1 && cnt <= 16) {
-                const float r2 = (mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(__ldg(&src[2].w), std2) : std2;
+                const float4 c = __ldg(&src[2]);
+                const float r2 =
+                    (mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, splat_colour_reach(c.x, c.y, c.z), std2) : std2;
                 const TileCull cull(a, q, r2);
                 mask = cnt == 16 ? 0xFFFFu : (1u << cnt) - 1u;
 #pragma unroll
@@ -566,7 +568,8 @@ __device__ __forceinline__ void stage_chunk(RasterShared &S, const gs_splat *__r
             c = __ldg(src + 2);
         }
         // Fragments beyond the r² limit cannot change the pixel (see splat_r2_bound).
-        const float lim = (MODE == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, std2) : std2;
+        const float lim =
+            (MODE == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, splat_colour_reach(c.x, c.y, c.z), std2) : std2;
         S.a[tid] = make_float4(a.x, a.y, lim, c.w);
         S.b[tid] = b;
         S.c[tid] = c;
