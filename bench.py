@@ -284,9 +284,94 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
     }
     sv.close()
     mv16.close()
+    out["multi_model"] = measure_multi_model(args, pods, stream)
+    out["ply_ingest"] = measure_ply_ingest(args)
     out["best_vs_plain_fp32"] = max(out["batched_fp32_fps"], out["batched_fp16_fps"], out["plain_fp16_fps"],
                                     out["served_fp16"]["fps"]) / plain_fps
     return out
+
+
+def measure_multi_model(args, pods, stream):
+    """Multi-model draw order at scale: one view of four models (0.5M, 1M, 1.5M, 3M Gaussians, each
+    with its own rigid transform, 10% carrying a per-Gaussian translation), drawn in key order."""
+    import torch
+
+    import gs300
+    from gs300 import scene as S
+
+    W, H = args.width, args.height
+    sh = stream.cuda_stream
+    rng = np.random.default_rng(5)
+    mv = gs300.MultiModelViewer()
+    keys = []
+    for i, n in enumerate((500_000, 1_000_000, 1_500_000, 3_000_000)):
+        k = f"m{i}"
+        mv.insert_model(k, S.synth_scene(n, seed=2 + i, translate_fraction=0.1))
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        mv.update_model_transform(k, tuple(rng.normal(0.0, 0.5, 3)), tuple(q), (1.0, 1.0, 1.0))
+        keys.append(k)
+    t = gs300.RenderTarget(W, H)
+    for k in range(3):
+        mv.update_camera_with_pod(pods[k])
+        mv.render(t, keys, stream=sh)
+        mv.synchronize(stream=sh)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = max(10, args.steps // 2)
+    e0.record(stream)
+    for k in range(reps):
+        mv.update_camera_with_pod(pods[k % 120])
+        mv.render(t, keys, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mv.synchronize(stream=sh)
+    ms = e0.elapsed_time(e1) / reps
+    mv.close()
+    return {"models": [500_000, 1_000_000, 1_500_000, 3_000_000], "fps": 1000.0 / ms, "ms": ms}
+
+
+def measure_ply_ingest(args):
+    """PLY ingest: a 1M-vertex standard 3DGS PLY (62 float properties, 248 B a vertex) converted
+    into FP32 records on the device (kernel alone, vertex block resident), and Viewer.from_ply
+    end to end from the file's bytes in host memory (header scan, one copy, conversion)."""
+    import torch
+
+    import gs300
+    from gs300 import records as R
+
+    n = 1_000_000
+    rng = np.random.default_rng(9)
+    names = (["x", "y", "z", "nx", "ny", "nz"] + [f"f_dc_{c}" for c in range(3)] +
+             [f"f_rest_{i}" for i in range(45)] + ["opacity"] + [f"scale_{i}" for i in range(3)] +
+             [f"rot_{i}" for i in range(4)])
+    v = rng.normal(0.0, 1.0, size=(n, len(names))).astype("<f4")
+    v[:, names.index("scale_0"):names.index("scale_0") + 3] -= 4.0
+    head = ["ply", "format binary_little_endian 1.0", f"element vertex {n}"]
+    head += [f"property float {x}" for x in names] + ["end_header"]
+    data = ("\n".join(head) + "\n").encode() + v.tobytes()
+    layout = gs300.ply_parse_header(data)
+    block = torch.from_numpy(np.frombuffer(data[layout.data_offset:], dtype=np.uint8).copy()).cuda()
+    recs = torch.empty(n * R.GAUSSIAN_POD_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        gs300.ply_convert(block.data_ptr(), layout, R.FORMAT_FP32, recs.data_ptr(), stream=s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(10):
+        gs300.ply_convert(block.data_ptr(), layout, R.FORMAT_FP32, recs.data_ptr(), stream=s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    kernel_ms = e0.elapsed_time(e1) / 10
+    moved = n * (layout.stride + R.GAUSSIAN_POD_DTYPE.itemsize)
+    t0 = time.perf_counter()
+    viewer = gs300.Viewer.from_ply(data)
+    e2e_s = time.perf_counter() - t0
+    viewer.close()
+    hbm_peak, _, _ = measured_peaks()
+    return {"vertices": n, "bytes_per_vertex": layout.stride, "kernel_ms": kernel_ms,
+            "kernel_gbs": moved / (kernel_ms / 1000.0) / 1e9,
+            "kernel_frac_hbm": moved / (kernel_ms / 1000.0) / 1e9 / hbm_peak,
+            "viewer_from_ply_ms": e2e_s * 1000.0, "viewer_from_ply_file_mb": len(data) / 1e6}
 
 
 def run_reference(args):
