@@ -545,6 +545,10 @@ def main():
         vis.append(v)
         pairs.append(p)
     prof = gs300.profile_read()
+    # the same frames again through the counting rasteriser, for the raster's work tallies
+    gs300.profile_enable(True, count=True)
+    for k in range(args.steps):
+        frame(k)
     counts = gs300.profile_counters()
     gs300.profile_enable(False)
     V = statistics.mean(vis)

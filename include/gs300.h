@@ -52,13 +52,16 @@ uint64_t gs_launch_count(void);
 /* Stage timers (no counterpart in the reference, whose timestamp queries are off,
  * src/radix_sorter.rs:504-507).  While enabled, CUDA events are recorded on the launching
  * stream around each stage: GS_PROF_PREPROCESS, _DEPTH_SORT, _BIN, _TILE_SORT, _RANGES,
- * _RASTER.  Enabling (or disabling) clears the accumulated times. */
+ * _RASTER.  Enabling (or disabling) clears the accumulated times.  enable: 0 = off, 1 = timers
+ * around the kernels every frame runs, 2 = timers, with splat-mode frames rasterised by a
+ * counting variant whose work tallies gs_profile_counters returns (its times are the counting
+ * kernel's, not the shipped one's). */
 #define GS_PROF_STAGES 6
 gs_status gs_profile_enable(int enable);
 /* Synchronises the device; ms[s] = summed stage time, launches[s] = timed launches. */
 gs_status gs_profile_read(double ms[GS_PROF_STAGES], uint32_t launches[GS_PROF_STAGES]);
-/* While profiling, splat-mode frames use a counting rasteriser; this returns its tallies since
- * gs_profile_enable (synchronises): pixel-splat evaluations, fragment alphas, channel-triple
+/* While profiling in mode 2, splat-mode frames use a counting rasteriser; this returns its tallies
+ * since gs_profile_enable (synchronises): pixel-splat evaluations, fragment alphas, channel-triple
  * blends, transmittance updates. */
 gs_status gs_profile_counters(uint64_t out[4]);
 

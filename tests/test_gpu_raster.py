@@ -135,3 +135,24 @@ def test_viewer_4k_matches_stage_path(gs, cuda, monkeypatch):
     got = pipe.render(u)
     assert gs.Renderer.status(pipe.r_scratch)[0] == 0
     assert np.array_equal(t.download(), got)
+
+
+def test_profile_modes_render_the_same_frame(gs, cuda):
+    """Stage timers (mode 1) run the shipped rasteriser and count nothing; counting mode (2) runs
+    the counting variant, which renders the same frame and tallies its work."""
+    sc = S.synth_scene(20_000, seed=23)
+    pipe = StagePipeline(gs, cuda, sc, R.FORMAT_FP32, 320, 200)
+    u = uniforms(gs, 320, 200, k=2, radius=5.0)
+    plain = pipe.render(u)
+    try:
+        gs.profile_enable(True)
+        timed = pipe.render(u)
+        assert sum(gs.profile_counters().values()) == 0
+        assert gs.profile_read()["raster"][1] >= 1
+        gs.profile_enable(True, count=True)
+        counted = pipe.render(u)
+        c = gs.profile_counters()
+    finally:
+        gs.profile_enable(False)
+    assert np.array_equal(plain, timed) and np.array_equal(plain, counted)
+    assert c["evaluations"] >= c["alphas"] > 0 and c["blends"] > 0

@@ -301,6 +301,7 @@ namespace {
 std::atomic<uint64_t> g_launches{0};
 std::mutex g_prof_mu;
 bool g_prof_on = false;
+bool g_prof_count = false;  // splat frames use the counting rasteriser
 struct StageEvents {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pairs;
     size_t used = 0;
@@ -319,7 +320,7 @@ void count_launches(uint32_t n) {
     else g_launches.fetch_add(n, std::memory_order_relaxed);
 }
 
-bool prof_enabled() { return g_prof_on; }
+bool prof_counting() { return g_prof_on && g_prof_count; }
 
 void prof_mark(int stage, bool begin, cudaStream_t st) {
     if (!g_prof_on || t_capturing) return;
@@ -368,6 +369,7 @@ gs_status gs_profile_enable(int enable) {
         e.open = false;
     }
     gs::g_prof_on = enable != 0;
+    gs::g_prof_count = enable == 2;
     return GS_OK;
 }
 

@@ -17,7 +17,8 @@ namespace gs {
 // the count of kernels this library has launched.
 enum ProfStage { kProfPreprocess = 0, kProfDepthSort, kProfBin, kProfTileSort, kProfRanges, kProfRaster, kProfStages };
 void prof_mark(int stage, bool begin, cudaStream_t st);
-bool prof_enabled();
+// Profiling in counting mode: splat frames run the counting rasteriser instead of the shipped one.
+bool prof_counting();
 // Work tallies of the counting rasteriser run while profiling: pixel-splat evaluations,
 // alphas, channel-triple blends, transmittance updates.
 cudaError_t raster_counters(unsigned long long out[4], bool reset);
@@ -122,6 +123,7 @@ struct RasterJob {
     const gs_splat *splats;
     const uint2 *pairs;
     const uint2 *ranges;
+    const uint32_t *order;  // launch order of the tiles (null: tile = CTA index)
     uint8_t *target;
     uint32_t W, H, pitch, tiles_x, max_splats, ntiles;
     Ctrl *ctrl;

@@ -23,6 +23,8 @@ namespace gs {
 
 constexpr uint32_t kBinThreads = 256;
 constexpr uint32_t kRasterThreads = 256;
+// A warp's pixel block is 8x4 pixels: its pixel centres span 7 x 3 pixels.
+constexpr float kBlockSpanX = 7.0f, kBlockSpanY = 3.0f;
 
 struct RasterLayout {
     Ctrl *ctrl;
@@ -34,6 +36,7 @@ struct RasterLayout {
     uint2 *ranges;       // per tile [start, end)
     uint32_t *counts;    // per tile pair count (counting path; null above kCountTiles tiles)
     uint32_t *blockcounts;  // per emit CTA and tile pair count (counting path)
+    uint32_t *order;     // tiles by descending pair count: the rasteriser's launch order (counting path)
     void *sort_scratch;
     uint32_t tiles_x, tiles_y, ntiles, key_bits;
 };
@@ -79,9 +82,11 @@ static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w
     p += align_up((size_t)max_pairs * 8, 256);
     L.ranges = reinterpret_cast<uint2 *>(p);
     p += align_up((size_t)L.ntiles * sizeof(uint2), 256);
-    L.counts = L.blockcounts = nullptr;
+    L.counts = L.blockcounts = L.order = nullptr;
     if (L.ntiles <= kCountTiles) {
         L.counts = reinterpret_cast<uint32_t *>(p);
+        p += align_up((size_t)L.ntiles * 4, 256);
+        L.order = reinterpret_cast<uint32_t *>(p);
         p += align_up((size_t)L.ntiles * 4, 256);
         L.blockcounts = reinterpret_cast<uint32_t *>(p);
         p += align_up((size_t)kEmitBlocks * L.ntiles * 4, 256);
@@ -97,7 +102,8 @@ size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_
            align_up((size_t)max_splats * 16, 256) + align_up((size_t)max_splats * 4 + 16, 256) +
            scan_flag_bytes(max_splats) + align_up((size_t)max_pairs * 8, 256) +
            align_up((size_t)tiles * sizeof(uint2), 256) +
-           (tiles <= kCountTiles ? align_up((size_t)tiles * 4, 256) + align_up((size_t)kEmitBlocks * tiles * 4, 256)
+           (tiles <= kCountTiles ? 2 * align_up((size_t)tiles * 4, 256) +
+                                       align_up((size_t)kEmitBlocks * tiles * 4, 256)
                                  : 0) +
            sort_pairs_scratch_bytes(max_pairs, key_bits);
 }
@@ -420,15 +426,29 @@ __global__ void __launch_bounds__(256) tile_count_kernel(const uint32_t *__restr
     if (c) atomicAdd(&counts[t], c);
 }
 
+// Size class of a tile list for the launch order: two classes per power of two, 0 = empty.
+constexpr uint32_t kOrderClasses = 66;
+__device__ __forceinline__ uint32_t order_class(uint32_t c) {
+    if (c == 0) return 0u;
+    const uint32_t lg = 31u - __clz(c);
+    return 1u + 2u * lg + (lg > 0 ? (c >> (lg - 1u)) & 1u : 0u);
+}
+
 // [start, end) of every tile from the per-tile counts (exclusive scan; one CTA, 8 tiles a
-// thread), and the tile-sort digit histograms, which are sums of those counts.
+// thread), the tile-sort digit histograms, which are sums of those counts, and the rasteriser's
+// launch order: tiles by descending size class (a counting sort), so the longest lists start
+// first and the grid does not end on a few long tiles that started late.  The order inside a
+// class is whatever the shared atomics give; it only schedules CTAs, every tile's pixels are
+// the same in any order.
 __global__ void __launch_bounds__(1024) tile_scan_kernel(const uint32_t *__restrict__ counts, uint32_t ntiles,
-                                                         uint2 *__restrict__ ranges, Ctrl *sort_ctrl,
-                                                         const PassSplit split) {
+                                                         uint2 *__restrict__ ranges, uint32_t *__restrict__ order,
+                                                         Ctrl *sort_ctrl, const PassSplit split) {
     __shared__ uint32_t s_w[32];
     __shared__ uint32_t s_h[4][256];
+    __shared__ uint32_t s_cls[kOrderClasses];
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     (&s_h[0][0])[tid] = 0u;
+    if (tid < kOrderClasses) s_cls[tid] = 0u;
     __syncthreads();
     const uint32_t base = tid * 8u;
     uint32_t v[8], sum = 0;
@@ -436,6 +456,7 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const uint32_t *__restr
     for (uint32_t j = 0; j < 8; ++j) {
         v[j] = base + j < ntiles ? counts[base + j] : 0u;
         sum += v[j];
+        if (base + j < ntiles) atomicAdd(&s_cls[order_class(v[j])], 1u);
         if (v[j])
             for (uint32_t p = 0; p < split.n; ++p)
                 atomicAdd(&s_h[p][((base + j) >> split.shift[p]) & ((1u << split.bits[p]) - 1u)], v[j]);
@@ -457,11 +478,22 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const uint32_t *__restr
         }
         s_w[lane] = xi - x;  // exclusive over warps
     }
+    if (tid == 32) {  // first position of each size class, largest class first
+        uint32_t at = 0;
+        for (int c = (int)kOrderClasses - 1; c >= 0; --c) {
+            const uint32_t k = s_cls[c];
+            s_cls[c] = at;
+            at += k;
+        }
+    }
     __syncthreads();
     uint32_t run = s_w[warp] + inc - sum;
 #pragma unroll
     for (uint32_t j = 0; j < 8; ++j) {
-        if (base + j < ntiles) ranges[base + j] = make_uint2(run, run + v[j]);
+        if (base + j < ntiles) {
+            ranges[base + j] = make_uint2(run, run + v[j]);
+            order[atomicAdd(&s_cls[order_class(v[j])], 1u)] = base + j;
+        }
         run += v[j];
     }
     const uint32_t p = tid >> 8, d = tid & 255u;
@@ -548,6 +580,7 @@ struct RasterShared {
     float4 b[kRasterThreads];    // q (or the point half sides)
     float4 c[kRasterThreads];    // s255.rgb
     float4 box[kRasterThreads];  // fragment box in pixel-centre coordinates
+    float2 inv[kRasterThreads];  // 1 / |Q·(7, 0)|², 1 / |Q·(0, 3)|² (the block edges in quad space)
     uint8_t list[kRasterThreads / 32][kRasterThreads];
     uint32_t kmin;
 };
@@ -574,10 +607,53 @@ __device__ __forceinline__ void stage_chunk(RasterShared &S, const gs_splat *__r
         S.b[tid] = b;
         S.c[tid] = c;
         S.box[tid] = make_float4(a.x - a.z, a.x + a.z, a.y - a.w, a.y + a.w);
+        if constexpr (MODE != GS_DISPLAY_POINT) {
+            const float e1x = b.x * kBlockSpanX, e1y = b.z * kBlockSpanX;
+            const float e2x = b.y * kBlockSpanY, e2y = b.w * kBlockSpanY;
+            S.inv[tid] = make_float2(__frcp_rn(e1x * e1x + e1y * e1y), __frcp_rn(e2x * e2x + e2y * e2y));
+        }
     }
 }
 
-// The calling warp's list of staged entries whose box meets its pixel block, in draw order.
+// Whether the fragment ellipse {p : |Q·(p - c)|² <= lim} of a staged splat meets the rectangle
+// of pixel centres [bx0, bx0 + 7] x [by0, by0 + 3] of a warp's block.  With c outside the
+// rectangle, the nearest point of the rectangle in the quadratic norm lies on an edge whose
+// half-plane c violates (moving from it toward c must leave the rectangle); Q maps each edge
+// to a segment in quad space, where the distance from the origin is minimised in closed form.
+// The limit carries a margin (0.2 % + 1e-4) above the rounding of either side, so a block
+// holding a pixel centre the fragment test accepts is never dropped; dropping the others
+// leaves every pixel unchanged.
+__device__ __forceinline__ bool seg_within(float ux, float uy, float ex, float ey, float inv, float lim) {
+    float t = -(ux * ex + uy * ey) * inv;
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    const float px = ux + t * ex, py = uy + t * ey;
+    return px * px + py * py <= lim;
+}
+
+__device__ __forceinline__ bool ellipse_meets_block(const float4 a, const float4 q, const float2 inv, float bx0,
+                                                    float bx1, float by0, float by1) {
+    const bool inx = a.x >= bx0 && a.x <= bx1, iny = a.y >= by0 && a.y <= by1;
+    if (inx && iny) return true;
+    const float lim = a.z * 1.002f + 1e-4f;
+    const float dx = bx0 - a.x, dy = by0 - a.y;
+    const float ux = q.x * dx + q.y * dy, uy = q.z * dx + q.w * dy;  // corner (bx0, by0)
+    const float e1x = q.x * kBlockSpanX, e1y = q.z * kBlockSpanX;   // along x, 7 px
+    const float e2x = q.y * kBlockSpanY, e2y = q.w * kBlockSpanY;   // along y, 3 px
+    bool m = false;
+    if (!inx) {  // left edge (c left of the block) or right edge
+        const bool left = a.x < bx0;
+        m = seg_within(left ? ux : ux + e1x, left ? uy : uy + e1y, e2x, e2y, inv.y, lim);
+    }
+    if (!iny && !m) {  // top edge (c above) or bottom edge
+        const bool top = a.y < by0;
+        m = seg_within(top ? ux : ux + e2x, top ? uy : uy + e2y, e1x, e1y, inv.x, lim);
+    }
+    return m;
+}
+
+// The calling warp's list of staged entries whose fragments can reach its pixel block, in draw
+// order: the fragment box, then (splat and ellipse modes) the ellipse itself must meet the block.
+template <uint32_t MODE>
 __device__ __forceinline__ uint32_t compact_chunk(RasterShared &S, uint32_t cnt, float bx0, float bx1, float by0,
                                                   float by1) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -589,6 +665,7 @@ __device__ __forceinline__ uint32_t compact_chunk(RasterShared &S, uint32_t cnt,
         if (j < cnt) {
             const float4 box = S.box[j];
             hit = !(box.y < bx0 || box.x > bx1 || box.w < by0 || box.z > by1);
+            if (MODE != GS_DISPLAY_POINT && hit) hit = ellipse_meets_block(S.a[j], S.b[j], S.inv[j], bx0, bx1, by0, by1);
         }
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, hit);
         if (hit) S.list[warp][nl + __popc(m & lt)] = (uint8_t)j;
@@ -637,7 +714,7 @@ __device__ __forceinline__ void raster_tile(
             const uint32_t cnt = min(kRasterThreads, n - base);
             stage_chunk<MODE>(S, sorted, pairs, s0 + base, cnt, std2, max_splats);
             __syncthreads();
-            const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
+            const uint32_t nl = compact_chunk<MODE>(S, cnt, bx0, bx1, by0, by1);
             for (uint32_t i = 0; i < nl; ++i) {
                 const uint32_t j = S.list[warp][i];
                 float al;
@@ -663,7 +740,7 @@ __device__ __forceinline__ void raster_tile(
             stage_chunk<MODE>(S, sorted, pairs, s0 + base, cnt, std2, max_splats);
             __syncthreads();
             if (__any_sync(0xFFFFFFFFu, !found)) {
-                const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
+                const uint32_t nl = compact_chunk<MODE>(S, cnt, bx0, bx1, by0, by1);
                 for (int i = (int)nl - 1; i >= 0; --i) {
                     if (__all_sync(0xFFFFFFFFu, found)) break;
                     const uint32_t j = S.list[warp][i];
@@ -711,7 +788,7 @@ __device__ __forceinline__ void raster_tile(
                 // k is uniform across the warp: a warp whose suffix starts past this chunk skips it
                 const bool inside = active && k < base + kRasterThreads;  // chunk holds suffix entries
                 if (__any_sync(0xFFFFFFFFu, inside)) {
-                    const uint32_t nl = compact_chunk(S, cnt, bx0, bx1, by0, by1);
+                    const uint32_t nl = compact_chunk<MODE>(S, cnt, bx0, bx1, by0, by1);
                     // Bounds that have met stay equal (same inputs, same operations), so once
                     // every started lane of the warp has met, one chain per channel suffices.
                     const bool met = d0 == h0 && d1 == h1 && d2 == h2;
@@ -782,13 +859,13 @@ __device__ __forceinline__ void raster_tile(
 
 
 template <uint32_t MODE, bool PORTABLE_EXP, bool COUNT>
-__global__ void __launch_bounds__(kRasterThreads) raster_kernel(const RasterJob J, float std2, float outline2,
+__global__ void __launch_bounds__(kRasterThreads, 6) raster_kernel(const RasterJob J, float std2, float outline2,
                                                                 uint32_t suffix_min, float eps,
                                                                 unsigned long long *counters) {
     __shared__ RasterShared S;
     raster_tile<MODE, PORTABLE_EXP, COUNT>(S, J.splats, J.pairs, J.ranges, J.target, J.W, J.H, J.pitch, J.tiles_x,
                                            std2, outline2, J.max_splats, suffix_min, eps, counters, J.ctrl,
-                                           blockIdx.x);
+                                           J.order ? J.order[blockIdx.x] : blockIdx.x);
 }
 
 // One grid over the tiles of several views (a batch): CTA b rasterises tile b - tile_base[v] of
@@ -806,9 +883,10 @@ __global__ void __launch_bounds__(kRasterThreads, 6) raster_views_kernel(const R
         else hi = mid - 1;
     }
     const RasterJob &J = jobs[lo];
+    const uint32_t b = blockIdx.x - tile_base[lo];
     raster_tile<MODE, PORTABLE_EXP, false>(S, J.splats, J.pairs, J.ranges, J.target, J.W, J.H, J.pitch, J.tiles_x,
                                            std2, outline2, J.max_splats, suffix_min, eps, nullptr, J.ctrl,
-                                           blockIdx.x - tile_base[lo]);
+                                           J.order ? J.order[b] : b);
 }
 
 // Work tallies of the counting raster variant (profiling only).
@@ -829,7 +907,7 @@ static void launch_raster_mode(const RasterJob &J, uint32_t ntiles, float std2, 
     if (exact) {
         raster_kernel<MODE, true, false><<<ntiles, kRasterThreads, 0, st>>>(J, std2, outline2, t.suffix_min, t.eps,
                                                                             nullptr);
-    } else if (MODE == GS_DISPLAY_SPLAT && prof_enabled()) {
+    } else if (MODE == GS_DISPLAY_SPLAT && prof_counting()) {
         unsigned long long *counts = nullptr;
         cudaGetSymbolAddress((void **)&counts, g_raster_counts);
         raster_kernel<GS_DISPLAY_SPLAT, false, true><<<ntiles, kRasterThreads, 0, st>>>(J, std2, outline2,
@@ -863,6 +941,7 @@ RasterJob raster_job(const RasterSegment *segs, uint32_t nseg, uint8_t *target, 
     J.max_splats = nseg == 1 ? segs[0].max_count : max_splats;
     J.pairs = L.pairs;
     J.ranges = L.ranges;
+    J.order = L.order;
     J.target = target;
     J.W = W;
     J.H = H;
@@ -951,7 +1030,7 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
         rank_offset += g.max_count;
     }
     if (L.counts) {
-        tile_scan_kernel<<<1, 1024, 0, st>>>(L.counts, L.ntiles, L.ranges, sort_ctrl, split);
+        tile_scan_kernel<<<1, 1024, 0, st>>>(L.counts, L.ntiles, L.ranges, L.order, sort_ctrl, split);
         count_launches(1);
     }
     prof_mark(kProfBin, false, st);

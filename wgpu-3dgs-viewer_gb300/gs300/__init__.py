@@ -55,8 +55,9 @@ def launch_count():
 PROFILE_STAGES = ("preprocess", "depth_sort", "bin", "tile_sort", "ranges", "raster")
 
 
-def profile_enable(on=True):
-    check(lib().gs_profile_enable(int(bool(on))))
+def profile_enable(on=True, count=False):
+    """Stage timers on or off; with count=True splat frames run the counting rasteriser."""
+    check(lib().gs_profile_enable((2 if count else 1) if on else 0))
 
 
 def profile_read():
@@ -68,7 +69,8 @@ def profile_read():
 
 
 def profile_counters():
-    """Rasteriser work tallies since profile_enable: evaluations, alphas, blends, transmittance."""
+    """Counting-rasteriser work tallies since profile_enable(count=True): evaluations, alphas,
+    blends, transmittance."""
     out = (ctypes.c_uint64 * 4)()
     check(lib().gs_profile_counters(ref(out)))
     return {"evaluations": out[0], "alphas": out[1], "blends": out[2], "transmittance": out[3]}
