@@ -65,10 +65,6 @@ __device__ __forceinline__ uint64_t pack_flag(uint32_t epoch, uint32_t status, u
     return ((uint64_t)epoch << 34) | ((uint64_t)status << 32) | (uint64_t)value;
 }
 
-__device__ __forceinline__ void st_release(uint64_t *p, uint64_t v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
 __device__ __forceinline__ void st_relaxed(uint64_t *p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -79,37 +75,9 @@ __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
     return v;
 }
 
-__device__ __forceinline__ uint64_t ld_acquire(const uint64_t *p) {
-    uint64_t v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// Exclusive look-back over predecessors j = tile-1 .. 0 of one counter whose flags live at
-// flags[j * stride].  Returns the exclusive prefix; on timeout sets the status bit.
-__device__ __forceinline__ uint32_t look_back(const uint64_t *flags, uint32_t stride, uint32_t tile,
-                                              uint32_t epoch, uint32_t *status) {
-    uint32_t prefix = 0;
-    int64_t j = (int64_t)tile - 1;
-    uint32_t spins = 0;
-    while (j >= 0) {
-        const uint64_t w = ld_acquire(flags + (uint64_t)j * stride);
-        const uint32_t ep = (uint32_t)(w >> 34);
-        const uint32_t st = (uint32_t)(w >> 32) & 3u;
-        if (ep != epoch || st == 0u) {
-            if (++spins > kSpinLimit) {
-                atomicOr(status, kStatusTimeout);
-                break;
-            }
-            if (spins > 64) __nanosleep(32);
-            continue;
-        }
-        prefix += (uint32_t)w;
-        if (st == kFlagPrefix) break;
-        --j;
-    }
-    return prefix;
-}
+// Look-back flags are published and read with relaxed atomics: a flag word carries everything
+// its reader uses (epoch, status and the count itself), and no other memory is read on the
+// strength of a flag, so no release/acquire ordering (and no fence) is needed.
 
 // Warp-cooperative look-back of one counter (flags[j], j < tile), called by all 32 lanes of a
 // warp: each round reads 32 predecessors at once, adds every aggregate down to the nearest
@@ -124,7 +92,7 @@ __device__ __forceinline__ uint32_t look_back_warp(const uint64_t *flags, uint32
         const int64_t j = hi - 1 - (int64_t)lane;
         uint64_t w;
         if (j >= 0) {
-            w = ld_acquire(flags + j);
+            w = ld_relaxed(flags + j);
         } else {
             w = pack_flag(epoch, kFlagPrefix, 0u);  // before the first tile: an empty prefix
         }

@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
             run += c;
         }
         s_base = run;  // block total until the look-back below
-        st_release(P.flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, run));
+        st_relaxed(P.flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, run));
     }
 
     // ---- per-instance vertex work (render.wesl:75-130), written at the Gaussian's index ----
@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
         const uint32_t total = s_base;
         const uint32_t prefix = tile == 0 ? 0u : look_back_warp(P.flags, tile, epoch, &P.ctrl->status);
         if (lane == 0) {
-            if (tile > 0) st_release(P.flags + tile, pack_flag(epoch, kFlagPrefix, prefix + total));
+            if (tile > 0) st_relaxed(P.flags + tile, pack_flag(epoch, kFlagPrefix, prefix + total));
             s_base = prefix;
             if (tile == P.ntiles - 1) {
                 // `post` (preprocess.wesl:108-126) and the DrawIndirectArgs instance count.
@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
             uint32_t total = 0;
             for (uint32_t w = 0; w < NW; ++w) total += __popc(s_bal[v][w]);
             s_base[v] = total;  // block total until the look-back
-            st_release(V.flags + tile, pack_flag(s_epoch[v], tile == 0 ? kFlagPrefix : kFlagAggregate, total));
+            st_relaxed(V.flags + tile, pack_flag(s_epoch[v], tile == 0 ? kFlagPrefix : kFlagAggregate, total));
         }
     }
     __syncthreads();
@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
         const uint32_t total = s_base[v];
         const uint32_t prefix = tile == 0 ? 0u : look_back_warp(V.flags, tile, s_epoch[v], &V.ctrl->status);
         if (lane == 0) {
-            if (tile > 0) st_release(V.flags + tile, pack_flag(s_epoch[v], kFlagPrefix, prefix + total));
+            if (tile > 0) st_relaxed(V.flags + tile, pack_flag(s_epoch[v], kFlagPrefix, prefix + total));
             s_base[v] = prefix;
             if (tile == P.ntiles - 1) {
                 const uint32_t c = prefix + total;
