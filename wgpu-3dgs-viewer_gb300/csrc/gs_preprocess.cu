@@ -12,8 +12,9 @@
 // 144 B.  Every thread reads its own row with 128-bit shared loads, so the 8 rows a quarter-warp
 // touches meet at most 2 to a bank (224-byte rows) or not at all (144-byte rows); dense
 // 128-byte rows would put a whole quarter-warp on one bank.  Visible Gaussians are compacted in ascending index
-// order with a warp ballot, a block scan and a decoupled look-back across CTAs (virtual CTA
-// ids from a ticket).
+// order with a warp ballot, a block scan and a decoupled look-back across CTAs (tile = CTA
+// index: CTAs are dispatched in index order, so a CTA only ever waits for CTAs already resident
+// or finished; every wait is bounded all the same).
 #include "gs_internal.h"
 
 namespace gs {
@@ -520,7 +521,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
 
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&P.ctrl->epoch;
-        s_tile = atomicAdd(&P.ctrl->ticket[0], 1u);
+        s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
         if (BULK) mbar_init(&s_bar, 1);
     }
     __syncthreads();

@@ -197,29 +197,30 @@ __global__ void __launch_bounds__(kBinThreads) bin_count_kernel(
     const uint32_t gi = sorted_index[k];
     uint32_t cnt = 0, x0 = 0, y0 = 0, w = 0, h = 0, mask = 0;
     if (gi < max_count) {
+        // all three 16-byte parts in one round trip (the colour bounds the corner-tile test)
         const float4 *src = reinterpret_cast<const float4 *>(splats + gi);
         const float4 a = __ldg(src);
         const float4 q = __ldg(src + 1);
+        const float4 c = __ldg(src + 2);
         if (!direct) {
             float4 *dst = reinterpret_cast<float4 *>(sorted_out + rank_offset + k);
             dst[0] = a;
             dst[1] = q;
-            dst[2] = __ldg(src + 2);
+            dst[2] = c;
         }
         if (tile_rect(a, tiles_x, tiles_y, &x0, &y0, &w, &h)) {
             cnt = w * h;
             // The footprint is convex and its box meets every tile of the rectangle, so only the
             // corner tiles of a rectangle (up to 16 tiles) can miss it; drop those that do.
             if (mode != GS_DISPLAY_POINT && cnt > 1 && cnt <= 16) {
-                const float4 c = __ldg(&src[2]);
                 const float r2 =
                     (mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, splat_colour_reach(c.x, c.y, c.z), std2) : std2;
                 const TileCull cull(a, q, r2);
                 mask = cnt == 16 ? 0xFFFFu : (1u << cnt) - 1u;
 #pragma unroll
-                for (uint32_t c = 0; c < 4; ++c) {
-                    const uint32_t tx = (c & 1u) ? w - 1 : 0u, ty = (c & 2u) ? h - 1 : 0u;
-                    if (((c & 1u) && w == 1) || ((c & 2u) && h == 1)) continue;  // same tile again
+                for (uint32_t corner = 0; corner < 4; ++corner) {
+                    const uint32_t tx = (corner & 1u) ? w - 1 : 0u, ty = (corner & 2u) ? h - 1 : 0u;
+                    if (((corner & 1u) && w == 1) || ((corner & 2u) && h == 1)) continue;  // same tile again
                     if (!cull.meets((float)((x0 + tx) * GS_TILE) + 0.5f, (float)((y0 + ty) * GS_TILE) + 0.5f))
                         mask &= ~(1u << (ty * w + tx));
                 }
@@ -240,7 +241,7 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
-        s_tile = atomicAdd(&ctrl->ticket[1], 1u);
+        s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
     }
     __syncthreads();
     const uint32_t n = count ? min(*count, max_count) : max_count;

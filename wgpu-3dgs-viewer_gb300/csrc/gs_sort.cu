@@ -5,7 +5,8 @@
 // block, stable.  The GB300 design differs: one global-histogram kernel reads the keys once
 // for all passes; each pass is a single kernel that ranks its block with warp ballots (so
 // equal digits keep input order), publishes per-digit counts and resolves the block's global
-// offsets by decoupled look-back (virtual block ids from an atomic ticket, every wait bounded),
+// offsets by decoupled look-back (block = CTA index: CTAs are dispatched in index order, so a
+// block waits only for blocks already resident or finished; every wait is bounded all the same),
 // then scatters through shared memory so that each digit's run is written contiguously.
 // The key count may live in device memory (the preprocess instance count), so a whole frame
 // can be enqueued (or graph-captured) without a host round trip.
@@ -166,7 +167,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
-        s_tile = atomicAdd(&ctrl->ticket[1 + pass], 1u);
+        s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
     }
     for (uint32_t k = tid; k < kSortWarps * 256; k += kSortThreads) (&s_whist[0][0])[k] = 0u;
     __syncthreads();
