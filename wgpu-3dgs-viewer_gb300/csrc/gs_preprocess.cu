@@ -47,7 +47,7 @@ struct PreViewsParams {
     uint32_t invert;
     const PreView *views;  // device array of nviews
     uint32_t nviews;
-    Ctrl *group;           // tile tickets of the launch (status of the record staging)
+    Ctrl *group;           // status of the record staging
 };
 
 // ---- FP32 math in the oracle's evaluation order ------------------------------------------
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t nv = P.nviews;
     if (tid == 0) {
-        s_tile = atomicAdd(&P.group->ticket[0], 1u);
+        s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
         if (FMT == GS_FORMAT_FP32) mbar_init(&s_bar, 1);
     }
     if (tid < nv) s_epoch[tid] = *(volatile uint32_t *)&P.views[tid].ctrl->epoch;
