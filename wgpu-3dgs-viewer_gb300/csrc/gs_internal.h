@@ -93,12 +93,13 @@ struct PassSplit {
 PassSplit even_split(uint32_t key_bits);
 
 // Packed (uint2 {key, value}) in-place sort for internal pair lists whose digit histograms
-// (split by even_split) the producer accumulated into the control block after sort_pairs_begin().
+// (split by even_split) the producer accumulated into the control block after sort_pairs_begin():
+// as counts, or (hist_scanned) already as exclusive digit offsets.
 size_t sort_pairs_scratch_bytes(uint32_t max_count, uint32_t key_bits);
 Ctrl *sort_pairs_ctrl(void *scratch);
 cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st);
 cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits,
-                              void *scratch, cudaStream_t st);
+                              void *scratch, cudaStream_t st, bool hist_scanned);
 
 // ---- K3 binning + K4 raster (gs_raster.cu) ----
 struct RasterSegment {

@@ -436,7 +436,8 @@ __device__ __forceinline__ uint32_t order_class(uint32_t c) {
 }
 
 // [start, end) of every tile from the per-tile counts (exclusive scan; one CTA, 8 tiles a
-// thread), the tile-sort digit histograms, which are sums of those counts, and the rasteriser's
+// thread), the tile sort's digit offsets (exclusive scans of the digit histograms, which are sums
+// of those counts), and the rasteriser's
 // launch order: tiles by descending size class (a counting sort), so the longest lists start
 // first and the grid does not end on a few long tiles that started late.  The order inside a
 // class is whatever the shared atomics give; it only schedules CTAs, every tile's pixels are
@@ -497,8 +498,21 @@ __global__ void __launch_bounds__(1024) tile_scan_kernel(const uint32_t *__restr
         }
         run += v[j];
     }
+    // the tile sort's digit offsets: per pass (256 threads each), the exclusive scan of its counts
+    __shared__ uint32_t s_hw[32];
     const uint32_t p = tid >> 8, d = tid & 255u;
-    if (p < split.n) sort_ctrl->hist[p][d] = s_h[p][d];
+    const uint32_t hv = s_h[p][d];
+    uint32_t hx = hv;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, hx, o);
+        if (lane >= o) hx += y;
+    }
+    if (lane == 31) s_hw[warp] = hx;
+    __syncthreads();
+    uint32_t hpre = 0;
+    for (uint32_t w = p * 8u; w < warp; ++w) hpre += s_hw[w];
+    if (p < split.n) sort_ctrl->hist[p][d] = hpre + hx - hv;
 }
 
 // K3d: advance the running pair base past a segment; flags a tile-pair list overflow.
@@ -1036,7 +1050,8 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
     }
     prof_mark(kProfBin, false, st);
     prof_mark(kProfTileSort, true, st);
-    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_scratch, st);
+    // counting path: tile_scan wrote the digit offsets already scanned; else the emit's counts
+    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_scratch, st, L.counts != nullptr);
     prof_mark(kProfTileSort, false, st);
     if (e != cudaSuccess) return e;
     merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, sort_ctrl);

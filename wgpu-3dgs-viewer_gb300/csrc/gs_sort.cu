@@ -29,6 +29,33 @@ __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t m
     return count ? min(*count, max_count) : max_count;
 }
 
+// Exclusive block scan of one value per thread (256 threads).  `tmp` holds 8 words.
+__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, uint32_t *total) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t t = lane < kSortWarps ? tmp[lane] : 0u;
+#pragma unroll
+        for (uint32_t o = 1; o < kSortWarps; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < kSortWarps) tmp[lane] = t;
+    }
+    __syncthreads();
+    const uint32_t before = warp ? tmp[warp - 1] : 0u;
+    *total = tmp[kSortWarps - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
 // Global digit histograms of all passes in one read of the keys (four keys per thread and
 // iteration, 16-byte loads when the keys are 16-byte aligned).  Per pass, the warp counts the
 // digit of lane 0 with one ballot (the high digits of float depth keys are nearly constant, and
@@ -80,33 +107,21 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
         const uint32_t v = h[p][threadIdx.x];
         if (v) atomicAdd(&ctrl->hist[p][threadIdx.x], v);
     }
-}
-
-// Exclusive block scan of one value per thread (256 threads).  `tmp` holds 8 words.
-__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, uint32_t *total) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) tmp[warp] = x;
+    // The last CTA to finish turns the histograms into exclusive digit offsets, once for every
+    // block of every pass.
+    __shared__ uint32_t s_last, s_tmp[kSortWarps];
+    __threadfence();
     __syncthreads();
-    if (warp == 0) {
-        uint32_t t = lane < kSortWarps ? tmp[lane] : 0u;
-#pragma unroll
-        for (uint32_t o = 1; o < kSortWarps; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, t, o);
-            if (lane >= o) t += y;
+    if (threadIdx.x == 0) s_last = atomicAdd(&ctrl->ticket[7], 1u) == gridDim.x - 1 ? 1u : 0u;
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (uint32_t p = 0; p < npasses; ++p) {
+            uint32_t total;
+            const uint32_t off = block_scan_excl(__ldcg(&ctrl->hist[p][threadIdx.x]), s_tmp, &total);
+            ctrl->hist[p][threadIdx.x] = off;
         }
-        if (lane < kSortWarps) tmp[lane] = t;
     }
-    __syncthreads();
-    const uint32_t before = warp ? tmp[warp - 1] : 0u;
-    *total = tmp[kSortWarps - 1];
-    __syncthreads();
-    return before + x - v;
 }
 
 // Look-back of one digit counter (flags[j * 256], j < tile) that polls up to four
@@ -156,7 +171,8 @@ template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
 __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
-    uint32_t max_count, uint32_t pass, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags) {
+    uint32_t max_count, uint32_t pass, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
+    uint32_t hist_scanned) {
     __shared__ uint2 s_kv[kTileKeys];
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_start[256];
@@ -240,7 +256,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
 
     uint32_t blk_total, hist_total;
     const uint32_t start = block_scan_excl(total, s_tmp, &blk_total);
-    const uint32_t goff = block_scan_excl(ctrl->hist[pass][d], s_tmp, &hist_total);
+    // the digit's first place in the output: the histograms hold exclusive offsets already
+    // when their producer scanned them (hist_scanned is uniform over the grid)
+    const uint32_t goff = hist_scanned ? ctrl->hist[pass][d] : block_scan_excl(ctrl->hist[pass][d], s_tmp, &hist_total);
     uint32_t prefix = 0;
     if (tile > 0 && live) {
         prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status);
@@ -375,25 +393,25 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
     const size_t fstride = (size_t)L.ntiles * 256;
     if (npasses == 1) {
         sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags);
+            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags, 1u);
         unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
         count_launches(2);
         return;
     }
     uint2 *src = L.alt_a, *dst = L.alt_b;
     sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags);
+        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags, 1u);
     for (uint32_t p = 1; p + 1 < npasses; ++p) {
         sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
             nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, 8u * p, pass_bits(key_bits, p), L.ctrl,
-            L.flags + p * fstride);
+            L.flags + p * fstride, 1u);
         uint2 *t = src;
         src = dst;
         dst = t;
     }
     sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
         nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, 8u * (npasses - 1),
-        pass_bits(key_bits, npasses - 1), L.ctrl, L.flags + (npasses - 1) * fstride);
+        pass_bits(key_bits, npasses - 1), L.ctrl, L.flags + (npasses - 1) * fstride, 1u);
     count_launches(npasses);
 }
 
@@ -428,7 +446,7 @@ cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st) {
 }
 
 cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits,
-                              void *scratch, cudaStream_t st) {
+                              void *scratch, cudaStream_t st, bool hist_scanned) {
     const uint32_t npasses = sort_passes(key_bits);
     if (max_count == 0) return cudaSuccess;
     SortLayout L = sort_layout(scratch, max_count, 1);
@@ -438,7 +456,8 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
     for (uint32_t p = 0; p < npasses; ++p) {
         sort_pass_kernel<true, true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
                                                                               count, max_count, p, split.shift[p],
-                                                                              split.bits[p], L.ctrl, L.flags + p * fstride);
+                                                                              split.bits[p], L.ctrl, L.flags + p * fstride,
+                                                                              hist_scanned ? 1u : 0u);
         uint2 *t = src;
         src = dst;
         dst = t;
