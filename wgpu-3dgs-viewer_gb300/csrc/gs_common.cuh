@@ -57,6 +57,12 @@ __device__ __forceinline__ void ctrl_reset(Ctrl *ctrl, int mode) {
         for (uint32_t k = t; k < 4 * 256; k += blockDim.x) (&ctrl->hist[0][0])[k] = 0u;
 }
 
+// L2 prefetch hint for a byte range (no data returned): 16-byte aligned address, size a
+// nonzero multiple of 16.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Look-back flag word: epoch (30 bits) | status (2 bits) | value (32 bits).
 constexpr uint32_t kFlagAggregate = 1u;
 constexpr uint32_t kFlagPrefix = 2u;

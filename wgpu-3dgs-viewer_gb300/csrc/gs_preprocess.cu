@@ -471,10 +471,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
 // 152 0.345 ms, 14 x 152 0.483 ms (prefetched records evicted before use).
 constexpr uint32_t kPrefetchTiles = 152 * 4;
 
-__device__ __forceinline__ void prefetch_l2(const void *src, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
-
 // Records [first, first + cnt) into shared rows: FP32 records by one bulk copy on the mbarrier
 // (phase 0, initialised by the caller before a __syncthreads), half records by 16-byte cp.async
 // chunks into padded rows.  Returns with the rows visible to every thread of the CTA.
@@ -489,12 +485,12 @@ __device__ __forceinline__ void stage_records(uint4 *s_rec, uint64_t *s_bar, con
         if (tid == 0) {
             mbar_expect_tx(s_bar, cnt * REC);
             bulk_g2s(s_rec, records + (size_t)first * REC, cnt * REC, s_bar);
-            if (prefetch_n > 0) prefetch_l2(records + (size_t)(first + kPrefetchTiles * kPreThreads) * REC, prefetch_n * REC);
+            if (prefetch_n > 0) prefetch_l2_bulk(records + (size_t)(first + kPrefetchTiles * kPreThreads) * REC, prefetch_n * REC);
         }
         if (!mbar_wait(s_bar, 0)) atomicOr(status, kStatusTimeout);
     } else {
         if (tid == 0 && prefetch_n > 0)
-            prefetch_l2(records + (size_t)(first + kPrefetchTiles * kPreThreads) * REC, prefetch_n * REC);
+            prefetch_l2_bulk(records + (size_t)(first + kPrefetchTiles * kPreThreads) * REC, prefetch_n * REC);
         // consecutive threads copy consecutive 16-byte chunks (coalesced); chunk q of the CTA
         // is chunk q % C16 of record q / C16
         const uint4 *src = reinterpret_cast<const uint4 *>(records + (size_t)first * REC);
