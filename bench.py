@@ -33,6 +33,10 @@ METRIC = "frames/s @6M splats 1080p"
 # launches each, averaged).  The preprocess reads every record once; the rasteriser's staged
 # splats come from L2, so its DRAM traffic is far below its algorithmic bytes.
 NCU_TRAFFIC_DEFAULT = {"raster_kernel": 144.2e6, "preprocess": 1.6577e9}
+# The rasteriser's share of the SM instruction-issue peak (ncu sm__inst_issued, % of peak sustained
+# elapsed, 1M-Gaussian 1080p frame): the limit it actually meets (FP32 FLOPs are a minority of its
+# instructions: shared loads, tests, rounding).
+NCU_ISSUE_RASTER = 0.854
 RECORD_BYTES = 224
 SPLAT_BYTES = 48
 
@@ -605,6 +609,9 @@ def main():
             "traffic": NCU_TRAFFIC_DEFAULT["raster_kernel"] if default_workload else None,
             "traffic_note": "DRAM bytes per launch (ncu), against algorithmic bytes "
             f"{dom['algo_bytes']:.3g}: staged splats are served from L2",
+            "issue_frac": NCU_ISSUE_RASTER,
+            "issue_note": "instructions issued / SM issue peak (ncu sm__inst_issued, 1M case): the kernel is "
+            "issue-bound, so this, not the FP32 FLOP fraction, is its distance to the hardware limit",
         }
     else:
         roofline = {
