@@ -1011,6 +1011,23 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
         if (e != cudaSuccess) return e;
     }
     const PassSplit split = even_split(L.key_bits);
+    // The emit kernel loops over its ranks grid-stride with equal shares per CTA: one resident
+    // wave (at most kEmitBlocks, the per-CTA count area) keeps a second, late wave from
+    // doubling the kernel's span.
+    const size_t emit_smem = L.counts ? (size_t)L.ntiles * 4u : 4u * 256u * 4u;
+    uint32_t emit_wave = kEmitBlocks;
+    {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            (L.counts ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bin_emit_kernel<true>, kBinThreads, emit_smem)
+                      : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bin_emit_kernel<false>, kBinThreads,
+                                                                       emit_smem)) == cudaSuccess &&
+            sms > 0 && per_sm > 0) {
+            const uint32_t wave = (uint32_t)sms * (uint32_t)per_sm;
+            if (wave < emit_wave) emit_wave = wave;
+        }
+    }
     uint32_t rank_offset = 0;
     prof_mark(kProfBin, true, st);
     const int direct = nseg == 1 ? 1 : 0;
@@ -1027,16 +1044,16 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
                                                          u.std_dev * u.std_dev, L.info, L.offsets);
         const uint32_t scan_blocks = (g.max_count + kScanTile - 1) / kScanTile;
         bin_scan_kernel<<<scan_blocks, 256, 0, st>>>(L.offsets, g.count, g.max_count, L.ctrl, L.flags);
-        const uint32_t eblocks = blocks < kEmitBlocks ? blocks : kEmitBlocks;
+        const uint32_t eblocks = blocks < emit_wave ? blocks : emit_wave;
         if (L.counts) {
-            bin_emit_kernel<true><<<eblocks, kBinThreads, L.ntiles * 4u, st>>>(
+            bin_emit_kernel<true><<<eblocks, kBinThreads, emit_smem, st>>>(
                 L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs, L.tiles_x, L.ntiles, L.ctrl, sort_ctrl,
                 split, L.blockcounts);
             tile_count_kernel<<<dim3((L.ntiles + 255) / 256, kCountSlices), 256, 0, st>>>(L.blockcounts, eblocks,
                                                                                          L.ntiles, L.counts);
             count_launches(1);
         } else {
-            bin_emit_kernel<false><<<eblocks, kBinThreads, 4u * 256u * 4u, st>>>(
+            bin_emit_kernel<false><<<eblocks, kBinThreads, emit_smem, st>>>(
                 L.info, L.offsets, g.count, g.max_count, L.pairs, max_pairs, L.tiles_x, L.ntiles, L.ctrl, sort_ctrl,
                 split, nullptr);
         }
