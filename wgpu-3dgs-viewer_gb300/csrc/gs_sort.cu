@@ -3,7 +3,8 @@
 // Same contract as the reference RadixSorter (src/radix_sorter.rs:56-96,658-669; kernels
 // src/shader/radix_sort.wgsl:78-529): 8-bit digits, least significant first, 3840 keys per
 // block, stable.  The GB300 design differs: one global-histogram kernel reads the keys once
-// for all passes; each pass is a single kernel that ranks its block with warp ballots (so
+// for all passes (its last CTA turns the histograms into exclusive digit offsets); each pass is
+// a single kernel that ranks its block warp by warp (match.any, or one ballot per digit bit, so
 // equal digits keep input order), publishes per-digit counts and resolves the block's global
 // offsets by decoupled look-back (block = CTA index: CTAs are dispatched in index order, so a
 // block waits only for blocks already resident or finished; every wait is bounded all the same),
