@@ -109,14 +109,14 @@ gs_status gs_gaussian_pack(const gs_gaussian *gaussians, size_t count, gs_gaussi
 /* Scan a PLY header (`len` bytes of the file, at least through "end_header\n") into `out`.
  * GS_ERR_INVALID_ARG for anything but binary_little_endian, a list property in or before the
  * vertex element, a missing or non-float required property, an f_rest count other than
- * 0, 9, 24 or 45, or a vertex stride above 4096 bytes.  Host only. */
+ * 0, 9, 24 or 45, or a vertex stride outside 4..1024 bytes.  Host only. */
 gs_status gs_ply_parse_header(const void *bytes, size_t len, gs_ply_layout *out_layout);
 
 /* Convert layout->count vertices at `vertices` (device memory, 4-byte aligned, holding
  * count·stride bytes: the file from data_offset on) into `records` (device memory, 16-byte
  * aligned, count records of `format`), on `stream`.  Asynchronous. */
 gs_status gs_ply_convert(const void *vertices, const gs_ply_layout *layout, uint32_t format,
-                         void *records, cudaStream_t stream);
+                         void *records, gs_stream stream);
 
 /* Derive the per-frame kernel uniforms (view-projection, model matrices, camera position,
  * decoded GaussianTransform) from the three pods and the viewport size.  The stage entry
@@ -138,8 +138,14 @@ gs_status gs_frame_uniforms_build(const gs_camera_pod *camera,
  * (src/radix_sorter.rs:931-934; GaussiansDepthBuffer::new, src/buffer/depth.rs:9-21). */
 uint32_t gs_depth_capacity(uint32_t n);
 
-/* Scratch areas of the stage calls must be zero-filled once before their first use; after
- * that they can be reused without clearing (their look-back flags carry a call epoch). */
+/* Scratch areas of the stage calls must be zero-filled once before their first use.  After
+ * that a scratch area can be reused by later calls of the same entry point without clearing,
+ * with any sizes (max_count, key_bits, max_splats, width, height, max_pairs) that its byte size
+ * covers: its control block and look-back flag arena sit at offsets no size moves, every flag
+ * carries the epoch of the call that wrote it, and a call whose flag arena is larger than the
+ * previous call's clears the difference on the device before reading any flag.  A scratch area
+ * belongs to one entry point (do not pass the same area to two different stage calls), and
+ * calls sharing one area must be ordered on the device (one stream, or synchronised). */
 
 /* Bytes of scratch gs_preprocess needs for `n` Gaussians. */
 size_t gs_preprocess_scratch_bytes(uint32_t n);
@@ -184,10 +190,13 @@ gs_status gs_radix_sort(uint32_t *keys, uint32_t *values, uint32_t max_count,
  * gs_radix_sort (stable, in place, bits [0, key_bits), device-side `count`), but its scratch is a
  * static device array inside the library: at most 1,048,576 (2^20) pairs per call, and every
  * device that loads the library holds about 19 MB for it until the process exits.  Larger
- * `max_count` returns GS_ERR_INVALID_ARG.  The first call on a device looks up the array's device
- * address and clears it on `stream`; make that first call before any stream capture.  All calls
- * share the one array, so calls whose work overlaps on the GPU (different streams, no ordering
- * between them) race: order them on one stream or synchronise between them. */
+ * `max_count` returns GS_ERR_INVALID_ARG.  Calls of any size and key width up to that limit may
+ * follow one another (the array is zero when the library loads and is then reused like any
+ * caller scratch).  The first call on a device looks up the array's device address with that
+ * device current (and caches it for the process); make that first call outside any stream
+ * capture.  All calls share the one array, so calls whose work overlaps on the GPU (different
+ * streams, no ordering between them) race: order them on one stream or synchronise between
+ * them. */
 gs_status gs_radix_sort_no_alloc(uint32_t *keys, uint32_t *values, uint32_t max_count,
                                  const uint32_t *count, uint32_t key_bits, gs_stream stream);
 
@@ -212,6 +221,16 @@ gs_status gs_rasterize(const gs_frame_uniforms *uniforms, const gs_splat *splats
  * GS_OK, GS_ERR_TIMEOUT or GS_ERR_CAPACITY.  Also reports the number of tile pairs the
  * last rasterisation produced when `pairs` is non-NULL. */
 gs_status gs_scratch_status(const void *scratch, gs_stream stream, uint32_t *pairs);
+
+/* Test hook for the bounded device waits (no counterpart in the reference, whose look-back spin
+ * is unbounded, src/shader/radix_sort.wgsl:382-403).  Every look-back of the stage calls and
+ * facades enqueued after this call polls a predecessor's flag at most `spin_limit` times before
+ * it records GS_ERR_TIMEOUT in its scratch status and carries on (writes whose addresses derive
+ * from a look-back stay bounds-checked, so a given-up wait yields a wrong but in-bounds result);
+ * with `stall_tile` other than 0xFFFFFFFF, the look-back tile (CTA) of that index publishes
+ * nothing, so its successors wait on a flag nothing sets and run out.  gs_debug_set_wait_fault(
+ * 4194304, 0xFFFFFFFF) restores the defaults.  spin_limit 0 is GS_ERR_INVALID_ARG. */
+gs_status gs_debug_set_wait_fault(uint32_t spin_limit, uint32_t stall_tile);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Viewer facade (src/lib.rs:64-275).  Owns device copies of the Gaussians and all buffers.  */

@@ -140,3 +140,11 @@ def test_tuning_default(gs):
     t = gs.tuning_default()
     assert t == {"suffix_min": 1536, "eps": pytest.approx(1e-6), "views_per_launch": 16, "streams": 16,
                  "sort_match": 1, "hist_blocks": 0, "raster_grid": 0}
+
+
+def test_wait_fault_hook_validates_and_restores(gs):
+    """gs_debug_set_wait_fault: a zero poll limit is rejected; the defaults can be restored."""
+    with pytest.raises(gs.GsError):
+        gs.debug_set_wait_fault(0, 1)
+    gs.debug_set_wait_fault(2000, 1)
+    gs.debug_set_wait_fault()

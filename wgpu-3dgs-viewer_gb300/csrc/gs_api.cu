@@ -322,6 +322,19 @@ void count_launches(uint32_t n) {
 
 bool prof_counting() { return g_prof_on && g_prof_count; }
 
+// Look-back configuration of every launch (spin limit in the low word, stalled tile in the high).
+namespace {
+std::atomic<uint64_t> g_wait_cfg{((uint64_t)kNoStall << 32) | kSpinLimit};
+}  // namespace
+
+WaitCfg wait_config() {
+    const uint64_t v = g_wait_cfg.load(std::memory_order_relaxed);
+    WaitCfg c;
+    c.spin_limit = (uint32_t)v;
+    c.stall_tile = (uint32_t)(v >> 32);
+    return c;
+}
+
 void prof_mark(int stage, bool begin, cudaStream_t st) {
     if (!g_prof_on || t_capturing) return;
     std::lock_guard<std::mutex> g(g_prof_mu);
@@ -576,6 +589,12 @@ gs_status gs_rasterize(const gs_frame_uniforms *u, const gs_splat *splats, const
     const int exact = getenv("GS300_EXACT_EXP") ? 1 : 0;
     const cudaError_t e = launch_raster(&seg, 1, *u, target, w, h, pitch, max_pairs, scratch, exact, (cudaStream_t)stream);
     return e == cudaSuccess ? GS_OK : cuda_fail(e, "gs_rasterize");
+}
+
+gs_status gs_debug_set_wait_fault(uint32_t spin_limit, uint32_t stall_tile) {
+    if (spin_limit == 0) return fail(GS_ERR_INVALID_ARG, "spin_limit must be >= 1");
+    gs::g_wait_cfg.store(((uint64_t)stall_tile << 32) | spin_limit, std::memory_order_relaxed);
+    return GS_OK;
 }
 
 gs_status gs_scratch_status(const void *scratch, gs_stream stream, uint32_t *pairs) {

@@ -13,34 +13,81 @@ constexpr uint32_t kStatusTimeout = 1u;
 constexpr uint32_t kStatusCapacity = 2u;
 constexpr uint32_t kStatusBounds = 4u;  // an index check failed; the access was skipped
 
-// Upper bound on polls of a look-back flag or an mbarrier before a kernel gives up, records
+// Default upper bound on polls of a look-back flag before a kernel gives up, records
 // kStatusTimeout and carries on with a garbage value (so that waiting successors also end).
+// The bound a launch uses is carried in its control block (Ctrl::spin_limit); mbarrier waits
+// use this constant.
 constexpr uint32_t kSpinLimit = 1u << 22;
 
-// Control block at the start of every scratch area.  `epoch` is bumped by the stage's init
-// kernel; look-back flags written under an older epoch read as "not yet published", so the
-// flag arrays never need clearing.
+// Look-back configuration of the launches a stage enqueues: the poll bound, and for testing the
+// bounded-wait path a look-back tile that never publishes its flags (kNoStall: none), so that
+// its successors' waits run out on a flag nothing sets.
+constexpr uint32_t kNoStall = 0xFFFFFFFFu;
+struct WaitCfg {
+    uint32_t spin_limit = kSpinLimit;
+    uint32_t stall_tile = kNoStall;
+};
+
+// Argument of ctrl_reset for a call that runs no arena-clearing kernel: leave the mark alone.
+constexpr uint32_t kKeepArena = 0xFFFFFFFFu;
+// Serial numbers above this restart at 0 with the whole arena cleared, so no epoch of a call
+// (at most a few per segment) ever wraps inside it.
+constexpr uint32_t kSerialRestart = (1u << 30) - (1u << 20);
+
+// Control block at a fixed offset of every scratch area.  Look-back flags live in the area's
+// flag arena, which starts right after the area's control blocks at an offset that no call size
+// moves; each flag word carries the epoch it was written under.  One counter per area (`serial`,
+// in the block that owns the area) hands out every epoch of that area, so a flag word left by an
+// earlier call, segment or stage of the area never carries the epoch a reader expects.  The
+// arena grows and shrinks with the call sizes, and the area's other buffers follow it: `clean`
+// counts the arena words known to hold only zeros or flag words; a call whose arena is larger
+// clears the words beyond it (clear_lo..clear_hi) in its first multi-CTA kernel, before any flag
+// is read, so stale payload of a larger earlier layout is never read as a published flag.
 struct Ctrl {
-    uint32_t epoch;
+    uint32_t epoch;       // epoch of this block's flags for the current call or segment
     uint32_t status;
     uint32_t ticket[8];
     uint32_t count;       // preprocess: V; raster: tile pairs kept
     uint32_t total;       // raster: tile pairs wanted (saturating)
     uint32_t pair_base;   // raster: running pair offset across segments
     uint32_t seg_total;   // raster: pairs of the segment being binned
-    uint32_t pad[2];
+    uint32_t serial;      // area owner: last epoch handed out in the area
+    uint32_t clean;       // area owner: leading arena words holding only zeros or flag words
+    uint32_t clear_lo;    // area owner: arena words [clear_lo, clear_hi) to clear in this call
+    uint32_t clear_hi;
+    uint32_t spin_limit;  // look-back poll bound of this call
+    uint32_t stall_tile;  // testing: look-back tile that never publishes (kNoStall: none)
+    uint32_t pad[4];
     uint32_t hist[4][256];  // sort: global digit histograms
 };
 static_assert(sizeof(Ctrl) % 16 == 0, "Ctrl must keep 16-byte alignment of what follows");
 
 // Resets a control block (one CTA): mode 1 = a new stage call (epoch, status, tickets, counters,
-// histograms); mode 0 = a new segment inside a call (epoch and tickets 0..1 only).  The epoch
-// tags every look-back flag, so flags of earlier calls never need clearing.
-__device__ __forceinline__ void ctrl_reset(Ctrl *ctrl, int mode) {
+// histograms, wait configuration); mode 0 = a new segment inside a call (epoch and tickets 0..1
+// only).  The epoch comes from `owner`, the block holding the area's serial counter (the block
+// itself for a single-stage area).  `arena_words` (owner, mode 1 only): words of the flag arena
+// this call uses, or kKeepArena when this call runs no clearing kernel.
+__device__ __forceinline__ void ctrl_reset(Ctrl *ctrl, int mode, Ctrl *owner, uint32_t arena_words, WaitCfg cfg) {
     const uint32_t t = threadIdx.x;
     if (t == 0) {
-        uint32_t e = ctrl->epoch + 1u;
-        if (e >= (1u << 30) || e == 0u) e = 1u;
+        if (ctrl == owner && mode == 1) {
+            if (owner->serial >= kSerialRestart) {
+                owner->serial = 0u;
+                owner->clean = 0u;  // flags of the old serial range may match new epochs
+            }
+            if (arena_words != kKeepArena) {
+                const uint32_t c = owner->clean;
+                owner->clear_lo = c < arena_words ? c : arena_words;
+                owner->clear_hi = arena_words;
+                // Past `arena_words` the area's other buffers begin, so only this call's arena
+                // is known clean once the clearing kernel has run.
+                owner->clean = arena_words;
+            } else {
+                owner->clear_lo = owner->clear_hi = 0u;
+            }
+        }
+        const uint32_t e = owner->serial + 1u;
+        owner->serial = e;
         ctrl->epoch = e;
         ctrl->ticket[0] = 0u;
         ctrl->ticket[1] = 0u;
@@ -51,10 +98,27 @@ __device__ __forceinline__ void ctrl_reset(Ctrl *ctrl, int mode) {
             ctrl->total = 0u;
             ctrl->pair_base = 0u;
             ctrl->seg_total = 0u;
+            ctrl->spin_limit = cfg.spin_limit;
+            ctrl->stall_tile = cfg.stall_tile;
         }
     }
     if (mode == 1)
         for (uint32_t k = t; k < 4 * 256; k += blockDim.x) (&ctrl->hist[0][0])[k] = 0u;
+}
+
+// The arena words this call must clear (set by the owner's mode-1 reset), cleared by every CTA
+// of a grid that runs before any look-back of the call (grid-stride, 16-byte stores).
+__device__ __forceinline__ void arena_clear(const Ctrl *owner, uint64_t *arena) {
+    const uint32_t lo = owner->clear_lo, hi = owner->clear_hi;
+    if (lo >= hi) return;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t a = (lo + 1u) & ~1u;  // first even word
+    if (a > hi) a = hi;
+    if (lo < a && blockIdx.x == 0 && threadIdx.x == 0) arena[lo] = 0ull;
+    const uint32_t b = a + ((hi - a) & ~1u);
+    for (uint32_t w = a + 2u * (blockIdx.x * blockDim.x + threadIdx.x); w < b; w += 2u * stride)
+        *reinterpret_cast<ulonglong2 *>(arena + w) = make_ulonglong2(0ull, 0ull);
+    if (b < hi && blockIdx.x == 0 && threadIdx.x == 0) arena[b] = 0ull;
 }
 
 // L2 prefetch hint for a byte range (no data returned): 16-byte aligned address, size a
@@ -75,6 +139,11 @@ __device__ __forceinline__ void st_relaxed(uint64_t *p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Publishes a look-back flag unless `tile` is the stalled tile of a bounded-wait test.
+__device__ __forceinline__ void publish_flag(uint64_t *p, uint32_t tile, uint32_t stall_tile, uint64_t v) {
+    if (tile != stall_tile) st_relaxed(p, v);
+}
+
 __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
     uint64_t v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -87,9 +156,11 @@ __device__ __forceinline__ uint64_t ld_relaxed(const uint64_t *p) {
 
 // Warp-cooperative look-back of one counter (flags[j], j < tile), called by all 32 lanes of a
 // warp: each round reads 32 predecessors at once, adds every aggregate down to the nearest
-// inclusive prefix and stops there.  Returns the exclusive prefix in every lane.
+// inclusive prefix and stops there.  Returns the exclusive prefix in every lane.  After
+// `limit` polls that find an unpublished predecessor it sets kStatusTimeout and returns what
+// it has summed.
 __device__ __forceinline__ uint32_t look_back_warp(const uint64_t *flags, uint32_t tile, uint32_t epoch,
-                                                   uint32_t *status) {
+                                                   uint32_t *status, uint32_t limit) {
     const uint32_t lane = threadIdx.x & 31u;
     uint32_t prefix = 0;
     int64_t hi = (int64_t)tile;  // window is [hi - 32, hi)
@@ -109,7 +180,7 @@ __device__ __forceinline__ uint32_t look_back_warp(const uint64_t *flags, uint32
         const uint32_t upto = pmask ? (uint32_t)(__ffs(pmask) - 1) : 31u;  // lanes 0..upto needed
         const uint32_t need = upto == 31u ? 0xFFFFFFFFu : ((2u << upto) - 1u);
         if (bad & need) {
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 if (lane == 0) atomicOr(status, kStatusTimeout);
                 break;
             }

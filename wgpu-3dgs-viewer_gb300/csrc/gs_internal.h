@@ -27,9 +27,14 @@ void count_launches(uint32_t n);
 // Records `message` as the calling thread's gs_last_error() and returns `status`.
 gs_status set_error(gs_status status, const char *message);
 
-// Resets a control block: mode 1 = a new stage call (epoch, status, tickets, counters,
-// histograms); mode 0 = a new segment inside a call (epoch and ticket[0] only).
-__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode);
+// Resets a control block (see ctrl_reset): owner = the block holding the area's epoch counter
+// and arena mark (nullptr: the block itself); arena_words = the flag-arena words of this call
+// for the owner's mode-1 reset, kKeepArena when no clearing kernel runs in the call.
+__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode, Ctrl *owner, uint32_t arena_words, WaitCfg cfg);
+
+// Look-back configuration every stage launch carries (the poll bound, and the stalled tile of
+// the bounded-wait test hook gs_debug_set_wait_fault).
+WaitCfg wait_config();
 
 // ---- K1 preprocess (gs_preprocess.cu) ----
 size_t preprocess_scratch_bytes(uint32_t n);
@@ -93,13 +98,14 @@ struct PassSplit {
 PassSplit even_split(uint32_t key_bits);
 
 // Packed (uint2 {key, value}) in-place sort for internal pair lists whose digit histograms
-// (split by even_split) the producer accumulated into the control block after sort_pairs_begin():
-// as counts, or (hist_scanned) already as exclusive digit offsets.
-size_t sort_pairs_scratch_bytes(uint32_t max_count, uint32_t key_bits);
-Ctrl *sort_pairs_ctrl(void *scratch);
-cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st);
-cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits,
-                              void *scratch, cudaStream_t st, bool hist_scanned);
+// (split by even_split) the producer accumulated into the control block `ctrl` after
+// sort_pairs_begin(): as counts, or (hist_scanned) already as exclusive digit offsets.  Its
+// look-back flags (sort_pairs_flag_words of them) lie in the flag arena of the area whose
+// control block `owner` is; `alt` holds max_count pairs.
+size_t sort_pairs_flag_words(uint32_t max_count, uint32_t key_bits);
+cudaError_t sort_pairs_begin(Ctrl *ctrl, Ctrl *owner, cudaStream_t st);
+cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits, Ctrl *ctrl,
+                              uint64_t *flags, uint2 *alt, cudaStream_t st, bool hist_scanned);
 
 // ---- K3 binning + K4 raster (gs_raster.cu) ----
 struct RasterSegment {

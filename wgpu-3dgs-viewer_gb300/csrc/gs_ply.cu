@@ -380,7 +380,7 @@ cudaError_t launch_ply_convert(const void *vertices, const gs_ply_layout &L, uin
 }  // namespace gs
 
 extern "C" gs_status gs_ply_convert(const void *vertices, const gs_ply_layout *layout, uint32_t format,
-                                    void *records, cudaStream_t stream) {
+                                    void *records, gs_stream stream) {
     const gs_status s = ply_check_layout(layout);
     if (s != GS_OK) return s;
     if (!(format == GS_FORMAT_FP32 || format == GS_FORMAT_HALF_SH_FP16 || format == GS_FORMAT_HALF_SH_BF16))

@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     constexpr uint32_t ROW16 = BULK ? C16 : C16 + 1;
     __shared__ __align__(16) uint4 s_rec[kPreThreads * ROW16];
     __shared__ __align__(8) uint64_t s_bar;
-    __shared__ uint32_t s_tile, s_epoch, s_base, s_warp[kPreThreads / 32];
+    __shared__ uint32_t s_tile, s_epoch, s_base, s_limit, s_stall, s_warp[kPreThreads / 32];
     __shared__ __align__(16) gs_frame_uniforms s_u;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if constexpr (DEV_UNIFORMS) {
@@ -531,6 +531,8 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
 
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&P.ctrl->epoch;
+        s_limit = P.ctrl->spin_limit;
+        s_stall = P.ctrl->stall_tile;
         s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
         if (BULK) mbar_init(&s_bar, 1);
     }
@@ -565,7 +567,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
             run += c;
         }
         s_base = run;  // block total until the look-back below
-        st_relaxed(P.flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, run));
+        publish_flag(P.flags + tile, tile, s_stall, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, run));
     }
 
     // ---- per-instance vertex work (render.wesl:75-130), written at the Gaussian's index ----
@@ -575,9 +577,9 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     __syncthreads();
     if (warp == 0) {
         const uint32_t total = s_base;
-        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(P.flags, tile, epoch, &P.ctrl->status);
+        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(P.flags, tile, epoch, &P.ctrl->status, s_limit);
         if (lane == 0) {
-            if (tile > 0) st_relaxed(P.flags + tile, pack_flag(epoch, kFlagPrefix, prefix + total));
+            if (tile > 0) publish_flag(P.flags + tile, tile, s_stall, pack_flag(epoch, kFlagPrefix, prefix + total));
             s_base = prefix;
             if (tile == P.ntiles - 1) {
                 // `post` (preprocess.wesl:108-126) and the DrawIndirectArgs instance count.
@@ -634,7 +636,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
     __shared__ uint32_t s_bal[kPreMaxViews][NW];
     __shared__ uint32_t s_base[kPreMaxViews];
     __shared__ uint32_t s_epoch[kPreMaxViews];
-    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_tile, s_limit, s_stall;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     const uint32_t nv = P.nviews;
     if (tid == 0) {
@@ -642,6 +644,10 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
         if (FMT == GS_FORMAT_FP32) mbar_init(&s_bar, 1);
     }
     if (tid < nv) s_epoch[tid] = *(volatile uint32_t *)&P.views[tid].ctrl->epoch;
+    if (tid == 0) {
+        s_limit = P.group->spin_limit;
+        s_stall = P.group->stall_tile;
+    }
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t first = tile * kPreThreads;
@@ -671,7 +677,8 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
             uint32_t total = 0;
             for (uint32_t w = 0; w < NW; ++w) total += __popc(s_bal[v][w]);
             s_base[v] = total;  // block total until the look-back
-            st_relaxed(V.flags + tile, pack_flag(s_epoch[v], tile == 0 ? kFlagPrefix : kFlagAggregate, total));
+            publish_flag(V.flags + tile, tile, s_stall,
+                         pack_flag(s_epoch[v], tile == 0 ? kFlagPrefix : kFlagAggregate, total));
         }
     }
     __syncthreads();
@@ -680,9 +687,9 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_views_kernel(const __g
     for (uint32_t v = warp; v < nv; v += NW) {
         const PreView &V = P.views[v];
         const uint32_t total = s_base[v];
-        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(V.flags, tile, s_epoch[v], &V.ctrl->status);
+        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(V.flags, tile, s_epoch[v], &V.ctrl->status, s_limit);
         if (lane == 0) {
-            if (tile > 0) st_relaxed(V.flags + tile, pack_flag(s_epoch[v], kFlagPrefix, prefix + total));
+            if (tile > 0) publish_flag(V.flags + tile, tile, s_stall, pack_flag(s_epoch[v], kFlagPrefix, prefix + total));
             s_base[v] = prefix;
             if (tile == P.ntiles - 1) {
                 const uint32_t c = prefix + total;
@@ -741,8 +748,11 @@ __global__ void preprocess_empty_kernel(uint32_t *indirect, uint32_t *dispatch, 
     }
 }
 
-__global__ void ctrl_init_views_kernel(const PreView *views, uint32_t nviews, Ctrl *group) {
-    ctrl_reset(blockIdx.x < nviews ? views[blockIdx.x].ctrl : group, 1);
+// A preprocess area holds its control block and look-back flags only, so no stale payload can
+// lie where a flag is read: its arena is never cleared (kKeepArena).
+__global__ void ctrl_init_views_kernel(const PreView *views, uint32_t nviews, Ctrl *group, WaitCfg cfg) {
+    Ctrl *c = blockIdx.x < nviews ? views[blockIdx.x].ctrl : group;
+    ctrl_reset(c, 1, c, kKeepArena, cfg);
 }
 
 __global__ void preprocess_views_empty_kernel(const PreView *views, uint32_t nviews) {
@@ -784,7 +794,7 @@ cudaError_t launch_preprocess_views(const void *records, uint32_t format, uint32
     if (nviews == 0) return cudaSuccess;
     if (nviews > kPreMaxViews) return cudaErrorInvalidValue;
     Ctrl *gctrl = reinterpret_cast<Ctrl *>(group);
-    ctrl_init_views_kernel<<<nviews + 1, 256, 0, st>>>(views, nviews, gctrl);
+    ctrl_init_views_kernel<<<nviews + 1, 256, 0, st>>>(views, nviews, gctrl, wait_config());
     count_launches(1);
     if (n == 0) {
         preprocess_views_empty_kernel<<<1, 32, 0, st>>>(views, nviews);
@@ -829,7 +839,7 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
                               const gs_frame_uniforms *u_dev) {
     Ctrl *ctrl = reinterpret_cast<Ctrl *>(scratch);
     uint64_t *flags = reinterpret_cast<uint64_t *>((uint8_t *)scratch + align_up(sizeof(Ctrl), 256));
-    ctrl_init_kernel<<<1, 256, 0, st>>>(ctrl, 1);
+    ctrl_init_kernel<<<1, 256, 0, st>>>(ctrl, 1, nullptr, kKeepArena, wait_config());
     count_launches(1);
     if (n == 0) {
         preprocess_empty_kernel<<<1, 1, 0, st>>>(indirect, dispatch, ctrl);

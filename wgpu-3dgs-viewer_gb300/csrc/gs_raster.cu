@@ -27,17 +27,20 @@ constexpr uint32_t kRasterThreads = 256;
 constexpr float kBlockSpanX = 7.0f, kBlockSpanY = 3.0f;
 
 struct RasterLayout {
-    Ctrl *ctrl;
+    Ctrl *ctrl;          // raster control block: owns the area's epoch counter and flag arena
+    Ctrl *sort_ctrl;     // tile sort control block
+    uint64_t *flags;     // flag arena, first part: scan look-back flags
+    uint64_t *sort_flags;  // flag arena, second part: tile-sort look-back flags
+    uint32_t arena_words;  // words of the flag arena (both parts)
     gs_splat *sorted;    // draw-ordered splats (several models), capacity max_splats
     uint4 *info;         // per draw rank: tile rectangle, kept-tile mask, pair value
     uint32_t *offsets;   // per draw rank: tile count, then its exclusive scan
-    uint64_t *flags;     // scan look-back flags
     uint2 *pairs;        // (tile, value), capacity max_pairs
     uint2 *ranges;       // per tile [start, end)
     uint32_t *counts;    // per tile pair count (counting path; null above kCountTiles tiles)
     uint32_t *blockcounts;  // per emit CTA and tile pair count (counting path)
     uint32_t *order;     // tiles by descending pair count: the rasteriser's launch order (counting path)
-    void *sort_scratch;
+    uint2 *sort_alt;     // the tile sort's ping-pong buffer, capacity max_pairs
     uint32_t tiles_x, tiles_y, ntiles, key_bits;
 };
 
@@ -56,10 +59,15 @@ static uint32_t bits_for(uint32_t v) {
     return b;
 }
 
-static size_t scan_flag_bytes(uint32_t max_splats) {
-    return align_up(((size_t)max_splats + kScanTile - 1) / kScanTile * 8 + 8, 256);
+// Scan flags: one per 4096-count tile (plus one), padded to 256 bytes so the tile-sort flags
+// after them stay 256-byte aligned.
+static size_t scan_flag_words(uint32_t max_splats) {
+    return align_up(((size_t)max_splats + kScanTile - 1) / kScanTile + 1, 32);
 }
 
+// Scratch: raster control block | tile-sort control block | flag arena (scan flags, tile-sort
+// flags) | buffers.  The two control blocks and the arena's start sit at offsets no call size
+// moves; the arena's length and everything after it follow (max_splats, width, height, max_pairs).
 static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w, uint32_t h,
                                   uint32_t max_pairs) {
     RasterLayout L;
@@ -70,14 +78,20 @@ static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w
     uint8_t *p = reinterpret_cast<uint8_t *>(scratch);
     L.ctrl = reinterpret_cast<Ctrl *>(p);
     p += align_up(sizeof(Ctrl), 256);
+    L.sort_ctrl = reinterpret_cast<Ctrl *>(p);
+    p += align_up(sizeof(Ctrl), 256);
+    const size_t scan_words = scan_flag_words(max_splats);
+    const size_t arena = scan_words + sort_pairs_flag_words(max_pairs, L.key_bits);
+    L.flags = reinterpret_cast<uint64_t *>(p);
+    L.sort_flags = L.flags + scan_words;
+    L.arena_words = (uint32_t)arena;
+    p += align_up(arena * sizeof(uint64_t), 256);
     L.sorted = reinterpret_cast<gs_splat *>(p);
     p += align_up((size_t)max_splats * sizeof(gs_splat), 256);
     L.info = reinterpret_cast<uint4 *>(p);
     p += align_up((size_t)max_splats * 16, 256);
     L.offsets = reinterpret_cast<uint32_t *>(p);
     p += align_up((size_t)max_splats * 4 + 16, 256);
-    L.flags = reinterpret_cast<uint64_t *>(p);
-    p += scan_flag_bytes(max_splats);
     L.pairs = reinterpret_cast<uint2 *>(p);
     p += align_up((size_t)max_pairs * 8, 256);
     L.ranges = reinterpret_cast<uint2 *>(p);
@@ -91,21 +105,22 @@ static RasterLayout raster_layout(void *scratch, uint32_t max_splats, uint32_t w
         L.blockcounts = reinterpret_cast<uint32_t *>(p);
         p += align_up((size_t)kEmitBlocks * L.ntiles * 4, 256);
     }
-    L.sort_scratch = p;
+    L.sort_alt = reinterpret_cast<uint2 *>(p);
     return L;
 }
 
 size_t raster_scratch_bytes(uint32_t max_splats, uint32_t w, uint32_t h, uint32_t max_pairs) {
     const uint32_t tiles = ((w + GS_TILE - 1) / GS_TILE) * ((h + GS_TILE - 1) / GS_TILE);
     const uint32_t key_bits = bits_for(tiles > 0 ? tiles - 1 : 0);
-    return align_up(sizeof(Ctrl), 256) + align_up((size_t)max_splats * sizeof(gs_splat), 256) +
-           align_up((size_t)max_splats * 16, 256) + align_up((size_t)max_splats * 4 + 16, 256) +
-           scan_flag_bytes(max_splats) + align_up((size_t)max_pairs * 8, 256) +
+    const size_t arena = scan_flag_words(max_splats) + sort_pairs_flag_words(max_pairs, key_bits);
+    return 2 * align_up(sizeof(Ctrl), 256) + align_up(arena * sizeof(uint64_t), 256) +
+           align_up((size_t)max_splats * sizeof(gs_splat), 256) + align_up((size_t)max_splats * 16, 256) +
+           align_up((size_t)max_splats * 4 + 16, 256) + align_up((size_t)max_pairs * 8, 256) +
            align_up((size_t)tiles * sizeof(uint2), 256) +
            (tiles <= kCountTiles ? 2 * align_up((size_t)tiles * 4, 256) +
                                        align_up((size_t)kEmitBlocks * tiles * 4, 256)
                                  : 0) +
-           sort_pairs_scratch_bytes(max_pairs, key_bits);
+           align_up((size_t)max_pairs * 8, 256);
 }
 
 const Ctrl *raster_ctrl(const void *scratch) { return reinterpret_cast<const Ctrl *>(scratch); }
@@ -185,11 +200,15 @@ struct TileCull {
 };
 
 // K3a: per draw rank, the splat's tile rectangle, the corner tiles its footprint misses, and
-// its tile count.  Several models first copy their splats into draw order.
+// its tile count.  Several models first copy their splats into draw order.  The first segment's
+// launch (arena non-null) also clears the flag-arena words the call must clear, before the
+// scan and the tile sort read any flag.
 __global__ void __launch_bounds__(kBinThreads) bin_count_kernel(
     const gs_splat *__restrict__ splats, const uint32_t *__restrict__ sorted_index, const uint32_t *count,
     uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, int direct, uint32_t tiles_x,
-    uint32_t tiles_y, uint32_t mode, float std2, uint4 *__restrict__ info, uint32_t *__restrict__ counts) {
+    uint32_t tiles_y, uint32_t mode, float std2, uint4 *__restrict__ info, uint32_t *__restrict__ counts,
+    const Ctrl *owner, uint64_t *arena) {
+    if (arena) arena_clear(owner, arena);
     const uint32_t n = count ? min(*count, max_count) : max_count;
     const uint32_t k = blockIdx.x * kBinThreads + threadIdx.x;
     if (k >= n) return;
@@ -237,10 +256,12 @@ __global__ void __launch_bounds__(kBinThreads) bin_count_kernel(
 __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ data, const uint32_t *count,
                                                        uint32_t max_count, Ctrl *ctrl, uint64_t *flags) {
     __shared__ uint32_t s_warp[8];
-    __shared__ uint32_t s_tile, s_epoch, s_prefix;
+    __shared__ uint32_t s_tile, s_epoch, s_prefix, s_limit, s_stall;
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
+        s_limit = ctrl->spin_limit;
+        s_stall = ctrl->stall_tile;
         s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
     }
     __syncthreads();
@@ -283,13 +304,14 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
             if (lane >= o) wi += y;
         }
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, wi, 7);
-        if (lane == 0) st_relaxed(flags + tile, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, total));
-        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(flags, tile, epoch, &ctrl->status);
+        if (lane == 0)
+            publish_flag(flags + tile, tile, s_stall, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, total));
+        const uint32_t prefix = tile == 0 ? 0u : look_back_warp(flags, tile, epoch, &ctrl->status, s_limit);
         if (lane < 8) s_warp[lane] = wi - wv;  // exclusive per-warp offsets
         if (lane == 0) {
             const uint64_t incl = (uint64_t)prefix + total;
             const uint32_t sat = incl > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)incl;
-            if (tile > 0) st_relaxed(flags + tile, pack_flag(epoch, kFlagPrefix, sat));
+            if (tile > 0) publish_flag(flags + tile, tile, s_stall, pack_flag(epoch, kFlagPrefix, sat));
             s_prefix = prefix;
             if (tile == ntiles - 1) ctrl->seg_total = sat;
         }
@@ -364,6 +386,12 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
             const uint32_t next = (k + 1 < n) ? offsets[k + 1] : seg_total;
             cnt = next - off;
             o = pair_base + off;
+            // A count beyond the splat's tile rectangle can only come from a scan whose
+            // look-back gave up (status already set): emit nothing for it.
+            if (next < off || cnt > (in.y & 0xFFFFu) * (in.y >> 16)) {
+                if (cnt) atomicOr(&const_cast<Ctrl *>(ctrl)->status, kStatusBounds);
+                cnt = 0;
+            }
         }
         const uint32_t x0 = in.x & 0xFFFFu, y0 = in.x >> 16, w = in.y & 0xFFFFu, h = in.y >> 16;
         if (cnt > 0 && cnt <= kWarpEmit) {
@@ -1001,11 +1029,16 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
     for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
     const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
     if (L.ntiles == 0) return cudaSuccess;
-    ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1);
+    // The first segment with splats clears the arena in its bin_count launch; with none, no kernel
+    // reads a flag and the arena mark stays.
+    bool any = false;
+    for (uint32_t s = 0; s < nseg; ++s) any = any || segs[s].max_count > 0;
+    const WaitCfg cfg = wait_config();
+    ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1, nullptr, any ? L.arena_words : kKeepArena, cfg);
     count_launches(1);
-    cudaError_t e = sort_pairs_begin(L.sort_scratch, st);
+    cudaError_t e = sort_pairs_begin(L.sort_ctrl, L.ctrl, st);
     if (e != cudaSuccess) return e;
-    Ctrl *sort_ctrl = sort_pairs_ctrl(L.sort_scratch);
+    Ctrl *sort_ctrl = L.sort_ctrl;
     if (L.counts) {
         e = cudaMemsetAsync(L.counts, 0, (size_t)L.ntiles * 4, st);
         if (e != cudaSuccess) return e;
@@ -1029,6 +1062,7 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
         }
     }
     uint32_t rank_offset = 0;
+    bool cleared = false;
     prof_mark(kProfBin, true, st);
     const int direct = nseg == 1 ? 1 : 0;
     for (uint32_t s = 0; s < nseg; ++s) {
@@ -1036,12 +1070,14 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
         const uint32_t blocks = (g.max_count + kBinThreads - 1) / kBinThreads;
         if (blocks == 0) continue;
         if (s > 0) {
-            ctrl_init_kernel<<<1, 32, 0, st>>>(L.ctrl, 0);
+            ctrl_init_kernel<<<1, 32, 0, st>>>(L.ctrl, 0, nullptr, kKeepArena, cfg);
             count_launches(1);
         }
         bin_count_kernel<<<blocks, kBinThreads, 0, st>>>(g.splats, g.sorted_index, g.count, g.max_count, rank_offset,
                                                          L.sorted, direct, L.tiles_x, L.tiles_y, u.display_mode,
-                                                         u.std_dev * u.std_dev, L.info, L.offsets);
+                                                         u.std_dev * u.std_dev, L.info, L.offsets, L.ctrl,
+                                                         cleared ? nullptr : L.flags);
+        cleared = true;
         const uint32_t scan_blocks = (g.max_count + kScanTile - 1) / kScanTile;
         bin_scan_kernel<<<scan_blocks, 256, 0, st>>>(L.offsets, g.count, g.max_count, L.ctrl, L.flags);
         const uint32_t eblocks = blocks < emit_wave ? blocks : emit_wave;
@@ -1068,7 +1104,8 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
     prof_mark(kProfBin, false, st);
     prof_mark(kProfTileSort, true, st);
     // counting path: tile_scan wrote the digit offsets already scanned; else the emit's counts
-    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_scratch, st, L.counts != nullptr);
+    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_ctrl, L.sort_flags, L.sort_alt, st,
+                          L.counts != nullptr);
     prof_mark(kProfTileSort, false, st);
     if (e != cudaSuccess) return e;
     merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, sort_ctrl);

@@ -24,7 +24,9 @@ constexpr uint32_t kTileKeys = kSortThreads * kSortRows;  // 3840
 constexpr uint32_t kSortWarps = kSortThreads / 32;
 static_assert(kTileKeys == GS_SORT_BLOCK_KVS, "block size must match the reference's");
 
-__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode) { ctrl_reset(ctrl, mode); }
+__global__ void ctrl_init_kernel(Ctrl *ctrl, int mode, Ctrl *owner, uint32_t arena_words, WaitCfg cfg) {
+    ctrl_reset(ctrl, mode, owner ? owner : ctrl, arena_words, cfg);
+}
 
 __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t max_count) {
     return count ? min(*count, max_count) : max_count;
@@ -73,11 +75,14 @@ __device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool va
     }
 }
 
+// Every CTA first clears its share of the flag-arena words this call must clear (the passes,
+// which are the arena's only readers, run after this kernel).
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restrict__ keys,
                                                         const uint32_t *count, uint32_t max_count,
-                                                        uint32_t key_bits, Ctrl *ctrl) {
+                                                        uint32_t key_bits, Ctrl *ctrl, uint64_t *arena) {
     __shared__ uint32_t h[4][256];
     const uint32_t npasses = (key_bits + 7u) / 8u;
+    arena_clear(ctrl, arena);
     for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&h[0][0])[k] = 0u;
     __syncthreads();
     const uint32_t n = load_count(count, max_count);
@@ -125,18 +130,19 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
     }
 }
 
-// Look-back of one digit counter (flags[j * 256], j < tile) that polls up to four
+// Look-back of one digit counter (flags[j * stride], j < tile) that polls up to four
 // predecessors per round trip.  The flag word carries everything the reader uses, so relaxed
-// loads suffice.  Returns the exclusive prefix; on timeout sets the status bit.
+// loads suffice.  Returns the exclusive prefix; after `limit` polls that find an unpublished
+// predecessor it sets the status bit and returns what it has summed.
 __device__ __forceinline__ uint32_t look_back_digit(const uint64_t *flags, uint32_t tile, uint32_t epoch,
-                                                    uint32_t *status) {
+                                                    uint32_t *status, uint32_t stride, uint32_t limit) {
     uint32_t prefix = 0;
     int64_t j = (int64_t)tile - 1;
     uint32_t spins = 0;
     while (j >= 0) {
         uint64_t w[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) w[q] = (j - q >= 0) ? ld_relaxed(flags + (uint64_t)(j - q) * 256u) : 0ull;
+        for (int q = 0; q < 4; ++q) w[q] = (j - q >= 0) ? ld_relaxed(flags + (uint64_t)(j - q) * stride) : 0ull;
         bool stalled = false, done = false;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -152,7 +158,7 @@ __device__ __forceinline__ uint32_t look_back_digit(const uint64_t *flags, uint3
         }
         if (done) break;
         if (stalled) {
-            if (++spins > kSpinLimit) {
+            if (++spins > limit) {
                 atomicOr(status, kStatusTimeout);
                 break;
             }
@@ -179,11 +185,13 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     __shared__ uint32_t s_start[256];
     __shared__ uint32_t s_gbase[256];
     __shared__ uint32_t s_tmp[kSortWarps];
-    __shared__ uint32_t s_tile, s_epoch;
+    __shared__ uint32_t s_tile, s_epoch, s_limit, s_stall;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     if (tid == 0) {
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
+        s_limit = ctrl->spin_limit;
+        s_stall = ctrl->stall_tile;
         s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
     }
     for (uint32_t k = tid; k < kSortWarps * 256; k += kSortThreads) (&s_whist[0][0])[k] = 0u;
@@ -250,10 +258,11 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     // Padding keys (all ones) rank last, in the largest digit.
     const uint32_t pub = (d == dmask) ? total - invalid : total;
     // Digits above dmask hold no key (padding keys sit in digit dmask), so only live digits
-    // publish and look back: a pass over 5 live bits touches 32 flags per block, not 256.
+    // publish and look back: a pass over 5 live bits keeps 32 flags per block, not 256.
     const bool live = d <= dmask;
-    uint64_t *f = flags + (size_t)tile * 256u + d;
-    if (live) st_relaxed(f, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
+    const uint32_t fstride = dmask + 1u;
+    uint64_t *f = flags + (size_t)tile * fstride + d;
+    if (live) publish_flag(f, tile, s_stall, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
 
     uint32_t blk_total, hist_total;
     const uint32_t start = block_scan_excl(total, s_tmp, &blk_total);
@@ -262,8 +271,8 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t goff = hist_scanned ? ctrl->hist[pass][d] : block_scan_excl(ctrl->hist[pass][d], s_tmp, &hist_total);
     uint32_t prefix = 0;
     if (tile > 0 && live) {
-        prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status);
-        st_relaxed(f, pack_flag(epoch, kFlagPrefix, prefix + pub));
+        prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status, fstride, s_limit);
+        publish_flag(f, tile, s_stall, pack_flag(epoch, kFlagPrefix, prefix + pub));
     }
     s_start[d] = start;
     s_gbase[d] = goff + prefix;
@@ -342,43 +351,60 @@ static inline uint32_t pass_bits(uint32_t key_bits, uint32_t p) {
     return left < 8u ? left : 8u;
 }
 
-struct SortLayout {
-    Ctrl *ctrl;
-    uint2 *alt_a, *alt_b;
-    uint64_t *flags;
-    uint32_t ntiles;
-};
+// Passes of the split-array sort: 8-bit digits from bit 0, the last one narrower when key_bits
+// is not a multiple of 8.
+static PassSplit lsd_split(uint32_t key_bits) {
+    PassSplit sp{};
+    sp.n = sort_passes(key_bits);
+    for (uint32_t p = 0; p < sp.n; ++p) {
+        sp.shift[p] = 8u * p;
+        sp.bits[p] = pass_bits(key_bits, p);
+    }
+    return sp;
+}
 
-// Scratch: control block | packed buffer A | packed buffer B (split sorts of 3+ passes only) |
-// look-back flags [passes][tiles][256].
 static size_t sort_tiles(uint32_t max_count) {
     size_t t = (max_count + kTileKeys - 1) / kTileKeys;
     return t ? t : 1;
 }
 
-static SortLayout sort_layout(void *scratch, uint32_t max_count, uint32_t npasses) {
+// Look-back flags of a sort: per pass, one word per block and live digit ([tiles][2^bits]).
+size_t sort_flag_words(uint32_t max_count, const PassSplit &sp) {
+    size_t w = 0;
+    for (uint32_t p = 0; p < sp.n; ++p) w += sort_tiles(max_count) << sp.bits[p];
+    return w;
+}
+
+struct SortLayout {
+    Ctrl *ctrl;
+    uint64_t *flags;  // the area's flag arena
+    uint2 *alt_a, *alt_b;
+    uint32_t ntiles;
+    size_t flag_words;
+};
+
+// Scratch: control block | flag arena (look-back flags of every pass) | packed buffer A | packed
+// buffer B (split sorts of 3+ passes only).  The control block and the arena start at offsets no
+// call size moves; the buffers after the arena follow its size.
+static SortLayout sort_layout(void *scratch, uint32_t max_count, const PassSplit &sp) {
     SortLayout L;
     uint8_t *p = reinterpret_cast<uint8_t *>(scratch);
     L.ntiles = (uint32_t)sort_tiles(max_count);
     L.ctrl = reinterpret_cast<Ctrl *>(p);
     p += align_up(sizeof(Ctrl), 256);
+    L.flags = reinterpret_cast<uint64_t *>(p);
+    L.flag_words = sort_flag_words(max_count, sp);
+    p += align_up(L.flag_words * sizeof(uint64_t), 256);
     L.alt_a = reinterpret_cast<uint2 *>(p);
     p += align_up((size_t)max_count * 8, 256);
     L.alt_b = reinterpret_cast<uint2 *>(p);
-    if (npasses >= 3) p += align_up((size_t)max_count * 8, 256);
-    L.flags = reinterpret_cast<uint64_t *>(p);
     return L;
 }
 
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits) {
-    const uint32_t np = sort_passes(key_bits);
-    return align_up(sizeof(Ctrl), 256) + (np >= 3 ? 2 : 1) * align_up((size_t)max_count * 8, 256) +
-           (size_t)np * sort_tiles(max_count) * 256 * sizeof(uint64_t);
-}
-
-size_t sort_pairs_scratch_bytes(uint32_t max_count, uint32_t key_bits) {
-    return align_up(sizeof(Ctrl), 256) + align_up((size_t)max_count * 8, 256) +
-           (size_t)sort_passes(key_bits) * sort_tiles(max_count) * 256 * sizeof(uint64_t);
+    const PassSplit sp = lsd_split(key_bits);
+    return align_up(sizeof(Ctrl), 256) + align_up(sort_flag_words(max_count, sp) * sizeof(uint64_t), 256) +
+           (sp.n >= 3 ? 2 : 1) * align_up((size_t)max_count * 8, 256);
 }
 
 static uint32_t grid_for(uint32_t max_count) {
@@ -389,82 +415,87 @@ static uint32_t grid_for(uint32_t max_count) {
 
 template <bool MATCH>
 static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
-                               uint32_t key_bits, const SortLayout &L, cudaStream_t st) {
-    const uint32_t npasses = sort_passes(key_bits);
-    const size_t fstride = (size_t)L.ntiles * 256;
+                               const PassSplit &sp, const SortLayout &L, cudaStream_t st) {
+    const uint32_t npasses = sp.n;
+    uint64_t *f = L.flags;
     if (npasses == 1) {
         sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags, 1u);
+            keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, sp.shift[0], sp.bits[0], L.ctrl, f, 1u);
         unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
         count_launches(2);
         return;
     }
     uint2 *src = L.alt_a, *dst = L.alt_b;
     sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, 0u, pass_bits(key_bits, 0), L.ctrl, L.flags, 1u);
+        keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, sp.shift[0], sp.bits[0], L.ctrl, f, 1u);
+    f += (size_t)L.ntiles << sp.bits[0];
     for (uint32_t p = 1; p + 1 < npasses; ++p) {
         sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, 8u * p, pass_bits(key_bits, p), L.ctrl,
-            L.flags + p * fstride, 1u);
+            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, sp.shift[p], sp.bits[p], L.ctrl, f, 1u);
+        f += (size_t)L.ntiles << sp.bits[p];
         uint2 *t = src;
         src = dst;
         dst = t;
     }
     sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, 8u * (npasses - 1),
-        pass_bits(key_bits, npasses - 1), L.ctrl, L.flags + (npasses - 1) * fstride, 1u);
+        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, sp.shift[npasses - 1],
+        sp.bits[npasses - 1], L.ctrl, f, 1u);
     count_launches(npasses);
 }
 
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage, const Tuning *tuning) {
     const Tuning tn = tuning ? *tuning : default_tuning();
-    const uint32_t npasses = sort_passes(key_bits);
-    const SortLayout L = sort_layout(scratch, max_count, npasses);
-    ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1);
+    const PassSplit sp = lsd_split(key_bits);
+    const SortLayout L = sort_layout(scratch, max_count, sp);
+    // With no pairs no kernel reads the flags, and none clears them: the arena mark stays.
+    ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1, nullptr, max_count ? (uint32_t)L.flag_words : kKeepArena,
+                                        wait_config());
     count_launches(1);
     if (max_count == 0) return cudaGetLastError();
     prof_mark(prof_stage, true, st);
     uint32_t hist_blocks = (max_count + 256 * 4 * 4 - 1) / (256 * 4 * 4);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
     if (tn.hist_blocks) hist_blocks = tn.hist_blocks < 152 * 8 ? tn.hist_blocks : 152 * 8;
-    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, key_bits, L.ctrl);
+    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, key_bits, L.ctrl, L.flags);
     count_launches(1);
     if (tn.sort_match)
-        launch_sort_passes<true>(keys, vals, max_count, count, key_bits, L, st);
+        launch_sort_passes<true>(keys, vals, max_count, count, sp, L, st);
     else
-        launch_sort_passes<false>(keys, vals, max_count, count, key_bits, L, st);
+        launch_sort_passes<false>(keys, vals, max_count, count, sp, L, st);
     prof_mark(prof_stage, false, st);
     return cudaGetLastError();
 }
 
-Ctrl *sort_pairs_ctrl(void *scratch) { return reinterpret_cast<Ctrl *>(scratch); }
+size_t sort_pairs_flag_words(uint32_t max_count, uint32_t key_bits) {
+    return sort_flag_words(max_count, even_split(key_bits));
+}
 
-cudaError_t sort_pairs_begin(void *scratch, cudaStream_t st) {
-    ctrl_init_kernel<<<1, 256, 0, st>>>(reinterpret_cast<Ctrl *>(scratch), 1);
+cudaError_t sort_pairs_begin(Ctrl *ctrl, Ctrl *owner, cudaStream_t st) {
+    ctrl_init_kernel<<<1, 256, 0, st>>>(ctrl, 1, owner, kKeepArena, wait_config());
     count_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits,
-                              void *scratch, cudaStream_t st, bool hist_scanned) {
-    const uint32_t npasses = sort_passes(key_bits);
-    if (max_count == 0) return cudaSuccess;
-    SortLayout L = sort_layout(scratch, max_count, 1);
+cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits, Ctrl *ctrl,
+                              uint64_t *flags, uint2 *alt, cudaStream_t st, bool hist_scanned) {
     const PassSplit split = even_split(key_bits);
-    const size_t fstride = (size_t)L.ntiles * 256;
-    uint2 *src = data, *dst = L.alt_a;
-    for (uint32_t p = 0; p < npasses; ++p) {
-        sort_pass_kernel<true, true, false><<<L.ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
-                                                                              count, max_count, p, split.shift[p],
-                                                                              split.bits[p], L.ctrl, L.flags + p * fstride,
-                                                                              hist_scanned ? 1u : 0u);
+    if (max_count == 0) return cudaSuccess;
+    const uint32_t ntiles = (uint32_t)sort_tiles(max_count);
+    uint2 *src = data, *dst = alt;
+    uint64_t *f = flags;
+    for (uint32_t p = 0; p < split.n; ++p) {
+        sort_pass_kernel<true, true, false><<<ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
+                                                                            count, max_count, p, split.shift[p],
+                                                                            split.bits[p], ctrl, f,
+                                                                            hist_scanned ? 1u : 0u);
+        f += (size_t)ntiles << split.bits[p];
         uint2 *t = src;
         src = dst;
         dst = t;
     }
-    count_launches(npasses);
-    if (npasses & 1u) {
+    count_launches(split.n);
+    if (split.n & 1u) {
         copy_packed_kernel<<<grid_for(max_count), 256, 0, st>>>(src, data, count, max_count);
         count_launches(1);
     }
@@ -473,13 +504,17 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
 
 // ---- allocation-free sort entry point -------------------------------------------------------
 // Scratch for gs_radix_sort_no_alloc lives in this file-scope device array instead of memory the
-// caller provides, so that entry point never allocates.  It is sized for kNoAllocMaxPairs pairs
-// of 32-bit keys (the 4-pass layout of sort_scratch_bytes) and every device that loads the
-// library holds it until the process exits.
+// caller provides, so that entry point never allocates.  It holds the largest layout the entry
+// point accepts (kNoAllocMaxPairs pairs of 32-bit keys, four passes) and every device that loads
+// the library holds it until the process exits.  A __device__ array without an initialiser is
+// zero when the module loads, which is the state a fresh scratch area needs; after that, calls of
+// any size and key width reuse it as any caller scratch is reused (the flag arena sits at a fixed
+// offset and is cleared where a call's layout grows past the previous one).
 constexpr uint32_t kNoAllocMaxPairs = 1u << 20;
 constexpr size_t kNoAllocTiles = (kNoAllocMaxPairs + kTileKeys - 1) / kTileKeys;
-constexpr size_t kNoAllocBytes = ((sizeof(Ctrl) + 255) / 256) * 256 + 2 * (((size_t)kNoAllocMaxPairs * 8 + 255) / 256) * 256 +
-                                 4 * kNoAllocTiles * 256 * sizeof(uint64_t);
+constexpr size_t kNoAllocBytes = ((sizeof(Ctrl) + 255) / 256) * 256 +
+                                 ((4 * kNoAllocTiles * 256 * sizeof(uint64_t) + 255) / 256) * 256 +
+                                 2 * (((size_t)kNoAllocMaxPairs * 8 + 255) / 256) * 256;
 static __device__ __align__(256) unsigned char g_no_alloc_scratch[kNoAllocBytes];
 
 namespace {
@@ -488,10 +523,10 @@ constexpr int kNoAllocDevices = 64;
 void *g_no_alloc_ptr[kNoAllocDevices] = {};
 }  // namespace
 
-// Device address of the array on the current device.  The first call on a device looks the
-// address up (in host code the array's name is only a stand-in, not a device address) and clears
-// the array on `st`; later calls reuse the cached address.
-static cudaError_t no_alloc_scratch(void **out, cudaStream_t st) {
+// Device address of the array on the current device.  In host code the array's name is only a
+// stand-in, not a device address: the first call on a device looks the address up with that
+// device current and caches it; later calls reuse it.
+static cudaError_t no_alloc_scratch(void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -500,8 +535,6 @@ static cudaError_t no_alloc_scratch(void **out, cudaStream_t st) {
     if (!g_no_alloc_ptr[dev]) {
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, g_no_alloc_scratch);
-        if (e != cudaSuccess) return e;
-        e = cudaMemsetAsync(p, 0, kNoAllocBytes, st);
         if (e != cudaSuccess) return e;
         g_no_alloc_ptr[dev] = p;
     }
@@ -520,9 +553,11 @@ extern "C" gs_status gs_radix_sort_no_alloc(uint32_t *keys, uint32_t *values, ui
                          "gs_radix_sort_no_alloc: max_count exceeds the static scratch limit of 1048576 pairs "
                          "(use gs_radix_sort with caller scratch)");
     if (max_count && (!keys || !values)) return set_error(GS_ERR_INVALID_ARG, "gs_radix_sort_no_alloc: NULL buffer");
+    if (sort_scratch_bytes(max_count, key_bits) > kNoAllocBytes)
+        return set_error(GS_ERR_INVALID_ARG, "gs_radix_sort_no_alloc: layout exceeds the static scratch");
     cudaStream_t st = (cudaStream_t)stream;
     void *scratch = nullptr;
-    cudaError_t e = no_alloc_scratch(&scratch, st);
+    cudaError_t e = no_alloc_scratch(&scratch);
     if (e == cudaSuccess) e = launch_sort(keys, values, max_count, count, key_bits, scratch, st);
     if (e != cudaSuccess) return set_error(GS_ERR_CUDA, cudaGetErrorString(e));
     return GS_OK;

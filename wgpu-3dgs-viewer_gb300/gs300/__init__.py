@@ -55,6 +55,17 @@ def launch_count():
 PROFILE_STAGES = ("preprocess", "depth_sort", "bin", "tile_sort", "ranges", "raster")
 
 
+SPIN_LIMIT_DEFAULT = 1 << 22
+NO_STALL = 0xFFFFFFFF
+
+
+def debug_set_wait_fault(spin_limit=SPIN_LIMIT_DEFAULT, stall_tile=NO_STALL):
+    """Test hook for the bounded device waits: look-backs enqueued afterwards poll at most
+    `spin_limit` times, and look-back tile `stall_tile` (if any) never publishes its flags, so
+    its successors' waits run out and report GS_ERR_TIMEOUT.  No arguments restore the defaults."""
+    check(lib().gs_debug_set_wait_fault(int(spin_limit), int(stall_tile)))
+
+
 def profile_enable(on=True, count=False):
     """Stage timers on or off; with count=True splat frames run the counting rasteriser."""
     check(lib().gs_profile_enable((2 if count else 1) if on else 0))

@@ -64,6 +64,7 @@ SIGNATURES = [
     ("gs_rasterize_scratch_bytes", SZ, [U32, U32, U32, U32]),
     ("gs_rasterize", ST, [P, P, P, P, U32, P, U32, U32, U32, U32, P, SZ, P]),
     ("gs_scratch_status", ST, [P, P, ctypes.POINTER(U32)]),
+    ("gs_debug_set_wait_fault", ST, [U32, U32]),
     ("gs_viewer_create", ST, [P, U32, U32, PP]),
     ("gs_viewer_create_from_ply", ST, [P, SZ, U32, PP]),
     ("gs_viewer_destroy", None, [P]),
