@@ -3,7 +3,8 @@
 Flags: -ffp-contract=off so every FP32 multiply and add rounds on its own (the evaluation
 order the CUDA kernels reproduce with -fmad=false); OpenMP for the CPU-baseline leg.
 gs_oracle64.cpp is the FP64 twin used as the precision tier's error reference;
-gs_oracle_ply.cpp restates the PLY vertex -> record conversion.
+gs_oracle_ply.cpp restates the PLY vertex -> record conversion; gs_oracle_wgpusort.cpp re-executes
+the reference's radix sorter workgroup by workgroup (the second sort oracle).
 """
 import os
 import subprocess
@@ -13,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgs_oracle.so")
-SRCS = [os.path.join(HERE, "gs_oracle.cpp"), os.path.join(HERE, "gs_oracle64.cpp"), os.path.join(HERE, "gs_oracle_ply.cpp")]
+SRCS = [os.path.join(HERE, "gs_oracle.cpp"), os.path.join(HERE, "gs_oracle64.cpp"), os.path.join(HERE, "gs_oracle_ply.cpp"),
+        os.path.join(HERE, "gs_oracle_wgpusort.cpp")]
 
 
 def build(force=False, verbose=False):

@@ -41,6 +41,8 @@ def _declare(L):
     L.oracle64_render.argtypes = [P, P, P, P, U, U, P, U, U, I]
     L.oracle64_render.restype = U
     L.oracle_ply_convert.argtypes = [P, P, U, P]
+    L.oracle_wgpu_radix_sort.argtypes = [P, U, P, U, U, U, I]
+    L.oracle_wgpu_radix_sort.restype = I
 
 
 def _p(a):
@@ -148,3 +150,16 @@ def exp_portable(x):
 
 def nproc():
     return os.cpu_count() or 1
+
+
+def wgpu_radix_sort(keys, payload, num_keys, dispatch_x, schedule=0):
+    """The reference sorter (RadixSorter::sort_indirect, src/radix_sorter.rs:658-669) re-executed
+    workgroup by workgroup on copies of `keys` (the depth buffer, u32) and `payload` (the index
+    buffer, u32): num_keys = the sorter state's N, dispatch_x = ceil(V / 3840).  Returns the two
+    buffers after the sort."""
+    k = np.ascontiguousarray(keys, dtype=np.uint32).copy()
+    p = np.ascontiguousarray(payload, dtype=np.uint32).copy()
+    rc = lib().oracle_wgpu_radix_sort(_p(k), len(k), _p(p), len(p), int(num_keys), int(dispatch_x), int(schedule))
+    if rc != 0:
+        raise RuntimeError("reference sorter restatement: a look-back met an unpublished predecessor")
+    return k, p

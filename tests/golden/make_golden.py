@@ -11,7 +11,8 @@ model_ply.npz — from the reference's own 9-Gaussian PLY fixture (coverage/mode
 synthetic_small.npz — a 600-Gaussian seeded scene rendered by the oracle at 96x64 in all
 three display modes (portable exp), to catch drift of the oracle itself.
 
-Usage: python tests/golden/make_golden.py [path/to/model.ply]
+Usage: python tests/golden/make_golden.py PATH/TO/coverage/model.ply
+(the reference checkout's 9-Gaussian PLY fixture; the path is required).
 """
 import math
 import os
@@ -59,7 +60,9 @@ def synthetic_frames():
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/coverage/model.ply"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py PATH/TO/coverage/model.ply (the reference's PLY fixture)")
+    src = sys.argv[1]
     verts = ply.read_vertices(src)
     g = ply.vertices_to_gaussians(verts)
     recs = S.pack_gaussians(g)

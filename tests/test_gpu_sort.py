@@ -2,7 +2,9 @@
 
 The reference RadixSorter is a stable LSD sort (src/radix_sorter.rs:73 builds it with
 subgroup size 1, so its in-block ranking is index-ordered), hence a stable sort by u32 key is
-its exact restatement."""
+its exact restatement; tests/test_oracle_wgpu_sort.py pins that by re-executing the reference
+sorter workgroup by workgroup, and the last test here holds the CUDA depth sort of a real
+preprocess output to that re-execution directly."""
 import numpy as np
 import pytest
 
@@ -131,3 +133,33 @@ def test_sort_full_size_properties(gs, cuda):
     same = sk[1:] == sk[:-1]
     assert bool((vals[1:][same] > vals[:-1][same]).all())
     assert bool((keys[vals.long()] == sk).all())
+
+
+def test_depth_sort_equals_reference_sorter_reexecution(gs, cuda, oracle):
+    """Preprocess -> sort through the stage entry points; the depth buffer and index buffer as the
+    preprocess left them (V keys, 2.0 pads up to the dispatch) go through the literal re-execution
+    of the reference sorter (num_keys = N, dispatch ceil(V / 3840)); the first V entries of both
+    must be identical."""
+    from gs300 import records as R
+    from gs300 import scene as S
+
+    from gpu_helpers import StagePipeline, uniforms
+
+    torch = cuda
+    for n, seed, radius in ((150_000, 3, 8.0), (20_000, 4, 5.0)):
+        p = StagePipeline(gs, torch, S.synth_scene(n, seed=seed), R.FORMAT_FP32, 640, 360)
+        p.preprocess(uniforms(gs, 640, 360, k=seed, radius=radius))
+        torch.cuda.synchronize()
+        v = p.count()
+        x = int(p.control[4].item())  # the sort dispatch {ceil(V/3840), 1, 1}
+        assert x == (v + 3839) // 3840
+        keys = p.depths.cpu().numpy().view(np.uint32).copy()
+        idx = p.indices.cpu().numpy().view(np.uint32).copy()
+        depth = np.zeros(4 * p.depth_cap, np.uint32)  # GaussiansDepthBuffer is 4 x keys_buffer_size
+        depth[: len(keys)] = keys
+        rk, rp = oracle.wgpu_radix_sort(depth, idx, n, x, 1)
+        p.sort()
+        torch.cuda.synchronize()
+        gk = p.depths.cpu().numpy().view(np.uint32)
+        gi = p.indices.cpu().numpy().view(np.uint32)
+        assert np.array_equal(gk[:v], rk[:v]) and np.array_equal(gi[:v], rp[:v])

@@ -587,7 +587,7 @@ gs_status gs_rasterize(const gs_frame_uniforms *u, const gs_splat *splats, const
         return fail(GS_ERR_INVALID_ARG, "scratch smaller than gs_rasterize_scratch_bytes");
     const RasterSegment seg{splats, sorted, count, max_splats};
     const int exact = getenv("GS300_EXACT_EXP") ? 1 : 0;
-    const cudaError_t e = launch_raster(&seg, 1, *u, target, w, h, pitch, max_pairs, scratch, exact, (cudaStream_t)stream);
+    const cudaError_t e = launch_raster(&seg, 1, raster_mode(*u), target, w, h, pitch, max_pairs, scratch, exact, (cudaStream_t)stream);
     return e == cudaSuccess ? GS_OK : cuda_fail(e, "gs_rasterize");
 }
 
@@ -635,7 +635,7 @@ gs_status viewer_render_locked(gs_viewer *v, uint8_t *target, uint32_t w, uint32
     if (s != GS_OK) return s;
     const RasterSegment seg{(const gs_splat *)v->model.splats.ptr, (const uint32_t *)v->model.indices.ptr,
                             v->model.indirect() + 1, v->model.n};
-    const cudaError_t e = launch_raster(&seg, 1, u, target, w, h, pitch, v->frame.max_pairs, v->frame.raster_scratch.ptr,
+    const cudaError_t e = launch_raster(&seg, 1, raster_mode(u), target, w, h, pitch, v->frame.max_pairs, v->frame.raster_scratch.ptr,
                                         v->frame.exact_exp, st);
     if (e != cudaSuccess) return cuda_fail(e, "raster launch");
     v->frame.last_target = target;
@@ -865,8 +865,8 @@ gs_status multi_render_locked(gs_multi_viewer *v, const std::vector<std::string>
         s = gs_frame_uniforms_build(&v->frame.camera, &identity, &v->frame.gt, w, h, &u);
         if (s != GS_OK) return s;
     }
-    // The raster only reads viewport, std dev and display mode, which all models share.
-    const cudaError_t e = launch_raster(segs.data(), (uint32_t)segs.size(), u, target, w, h, pitch, v->frame.max_pairs,
+    // Binning and raster read only std dev and display mode (RasterMode), which all models share.
+    const cudaError_t e = launch_raster(segs.data(), (uint32_t)segs.size(), raster_mode(u), target, w, h, pitch, v->frame.max_pairs,
                                         v->frame.raster_scratch.ptr, v->frame.exact_exp, st);
     if (e != cudaSuccess) return cuda_fail(e, "raster launch");
     v->last_keys = keys;
@@ -1268,11 +1268,13 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
                 if (err == cudaSuccess) {
                     const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1,
                                             ms[i]->n};
+                    // The graph is replayed for later cameras: binning and raster take only the
+                    // display mode and std dev, which are part of the shape key (frame.gt).
                     if (b->tuning.raster_grid)
-                        err = launch_binning(&seg, 1, uh[i], views[i].width, views[i].height, v.max_pairs,
+                        err = launch_binning(&seg, 1, raster_mode(uh[i]), views[i].width, views[i].height, v.max_pairs,
                                              v.raster_scratch.ptr, vs);
                     else
-                        err = launch_raster(&seg, 1, uh[i], views[i].target, views[i].width, views[i].height,
+                        err = launch_raster(&seg, 1, raster_mode(uh[i]), views[i].target, views[i].width, views[i].height,
                                             views[i].pitch, v.max_pairs, v.raster_scratch.ptr, mv->frame.exact_exp, vs,
                                             &b->tuning);
                 }
@@ -1285,7 +1287,7 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
         if (err == cudaSuccess && b->tuning.raster_grid)
             err = launch_raster_views(reinterpret_cast<const RasterJob *>(b->jobs_dev.ptr),
                                       reinterpret_cast<const uint32_t *>(b->tile_base_dev.ptr), n, tile_base[n],
-                                      uh[0], mv->frame.exact_exp, b->capture, &b->tuning);
+                                      raster_mode(uh[0]), mv->frame.exact_exp, b->capture, &b->tuning);
         t_capturing = false;
         cudaGraph_t graph = nullptr;
         const cudaError_t end = cudaStreamEndCapture(b->capture, &graph);
@@ -1661,7 +1663,7 @@ gs_status server_finish(gs_server *sv, ServerReq &r, ServerSlot &sl, uint8_t *ta
                                 v.sort_scratch.ptr, sl.stream);
     if (e == cudaSuccess) {
         const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
-        e = launch_raster(&seg, 1, u, target, r.w, r.h, pitch, v.max_pairs, v.raster_scratch.ptr,
+        e = launch_raster(&seg, 1, raster_mode(u), target, r.w, r.h, pitch, v.max_pairs, v.raster_scratch.ptr,
                           sv->mv->frame.exact_exp, sl.stream);
     }
     if (e == cudaSuccess && r.out_on_host && r.out)

@@ -108,6 +108,14 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
                               uint64_t *flags, uint2 *alt, cudaStream_t st, bool hist_scanned);
 
 // ---- K3 binning + K4 raster (gs_raster.cu) ----
+// The only frame uniforms binning and rasterisation read: camera, model and SH fields never
+// reach them, so a captured graph of these launches stays valid for any camera.
+struct RasterMode {
+    uint32_t display_mode;
+    float std_dev;
+};
+inline RasterMode raster_mode(const gs_frame_uniforms &u) { return RasterMode{u.display_mode, u.std_dev}; }
+
 struct RasterSegment {
     const gs_splat *splats;       // indexed by Gaussian index
     const uint32_t *sorted_index; // draw order
@@ -116,7 +124,7 @@ struct RasterSegment {
 };
 size_t raster_scratch_bytes(uint32_t max_splats, uint32_t width, uint32_t height, uint32_t max_pairs);
 // exact_exp: 1 = the portable exp (bit-identical with the CPU oracle), 0 = the SFU exp.
-cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u,
+cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const RasterMode &u,
                           uint8_t *target, uint32_t width, uint32_t height, uint32_t pitch,
                           uint32_t max_pairs, void *scratch, int exact_exp, cudaStream_t st,
                           const Tuning *tuning = nullptr);
@@ -139,12 +147,12 @@ RasterJob raster_job(const RasterSegment *segs, uint32_t nseg, uint8_t *target, 
                      uint32_t pitch, uint32_t max_pairs, void *scratch);
 // Binning, tile sort and tile ranges of one view (everything launch_raster does before the
 // rasteriser itself).
-cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint32_t width,
+cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t width,
                            uint32_t height, uint32_t max_pairs, void *scratch, cudaStream_t st);
 // One rasteriser grid over several binned views (same display mode and std): tile_base holds the
 // prefix of the views' tile counts (nviews + 1 entries, device), jobs the views (device).
 cudaError_t launch_raster_views(const RasterJob *jobs, const uint32_t *tile_base, uint32_t nviews,
-                                uint32_t total_tiles, const gs_frame_uniforms &u, int exact_exp, cudaStream_t st,
+                                uint32_t total_tiles, const RasterMode &u, int exact_exp, cudaStream_t st,
                                 const Tuning *tuning = nullptr);
 
 }  // namespace gs

@@ -996,7 +996,7 @@ RasterJob raster_job(const RasterSegment *segs, uint32_t nseg, uint8_t *target, 
 }
 
 cudaError_t launch_raster_views(const RasterJob *jobs_dev, const uint32_t *tile_base_dev, uint32_t nviews,
-                                uint32_t total_tiles, const gs_frame_uniforms &u, int exact_exp, cudaStream_t st,
+                                uint32_t total_tiles, const RasterMode &u, int exact_exp, cudaStream_t st,
                                 const Tuning *tuning) {
     if (nviews == 0 || total_tiles == 0) return cudaSuccess;
     const Tuning tn = tuning ? *tuning : default_tuning();
@@ -1023,7 +1023,7 @@ cudaError_t launch_raster_views(const RasterJob *jobs_dev, const uint32_t *tile_
     return cudaGetLastError();
 }
 
-cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint32_t W,
+cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t W,
                            uint32_t H, uint32_t max_pairs, void *scratch, cudaStream_t st) {
     uint32_t max_splats = 0;
     for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
@@ -1124,7 +1124,7 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const gs_fr
     return cudaGetLastError();
 }
 
-cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const gs_frame_uniforms &u, uint8_t *target,
+cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint8_t *target,
                           uint32_t W, uint32_t H, uint32_t pitch, uint32_t max_pairs, void *scratch, int exact_exp,
                           cudaStream_t st, const Tuning *tuning) {
     const Tuning tn = tuning ? *tuning : default_tuning();
