@@ -55,13 +55,19 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tiers", action="store_true")
     ap.add_argument("--batch-views", type=int, default=8)
-    ap.add_argument("--serve-inflight", type=int, default=4)
+    ap.add_argument("--serve-inflight", type=int, default=8)
     ap.add_argument("--serve-wait-ms", type=float, default=0.0,
                     help="dynamic batching window of the served tier (0 = admit as soon as a slot frees)")
     ap.add_argument("--precision", action="store_true",
                     help="precision report instead of the benchmark: FP32 and half records against "
                     "the host FP64 oracle over --precision-cameras orbit cameras")
     ap.add_argument("--precision-cameras", type=int, default=32)
+    ap.add_argument("--precision-sample-cameras", type=int, default=4,
+                    help="cameras of the precision sample in the default run (0 = none)")
+    ap.add_argument("--config-views", type=int, default=64, help="views per launch of the batching configuration")
+    ap.add_argument("--serve-requests", type=int, default=1000, help="requests per offered rate of the serving sweep")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[200, 500, 1000, 1500, 2000],
+                    help="offered request rates (req/s) of the serving sweep")
     return ap.parse_args()
 
 
@@ -288,33 +294,54 @@ def measure_tiers(args, scene, pods, stream, plain_fps):
     }
     sv.close()
     mv16.close()
-    out["multi_model"] = measure_multi_model(args, pods, stream)
+    cfg_mv, cfg_keys = config_models()
+    out["multi_model"] = measure_multi_model(args, cfg_mv, cfg_keys, pods, stream)
+    out["batched_config"] = measure_batched_config(args, cfg_mv, cfg_keys, stream)
+    cfg_mv.close()
+    out["served_config"] = measure_served_config(args, stream)
     out["ply_ingest"] = measure_ply_ingest(args)
+    if args.precision_sample_cameras > 0:
+        out["precision"] = measure_precision_sample(args, {R.FORMAT_FP32: scene, R.FORMAT_HALF_SH_BF16: half},
+                                                    lambda k: pods[k % 120])
     out["best_vs_plain_fp32"] = max(out["batched_fp32_fps"], out["batched_fp16_fps"], out["plain_fp16_fps"],
                                     out["served_fp16"]["fps"]) / plain_fps
     return out
 
 
-def measure_multi_model(args, pods, stream):
-    """Multi-model draw order at scale: one view of four models (0.5M, 1M, 1.5M, 3M Gaussians, each
-    with its own rigid transform, 10% carrying a per-Gaussian translation), drawn in key order."""
-    import torch
+BATCH_MODELS = (500_000, 1_000_000, 1_500_000, 3_000_000)
+BATCH_RES = ((640, 360), (1280, 720), (1920, 1080), (3840, 2160))
+SERVE_RES = ((1280, 720), (1920, 1080), (3840, 2160))
 
+
+def config_models():
+    """The batching configuration's models: 0.5M, 1M, 1.5M and 3M Gaussians of the plain
+    distributions, each with a random rigid model transform, 10% of the Gaussians carrying a
+    per-Gaussian translation N(0, 0.1²)."""
     import gs300
     from gs300 import scene as S
 
-    W, H = args.width, args.height
-    sh = stream.cuda_stream
     rng = np.random.default_rng(5)
     mv = gs300.MultiModelViewer()
     keys = []
-    for i, n in enumerate((500_000, 1_000_000, 1_500_000, 3_000_000)):
+    for i, n in enumerate(BATCH_MODELS):
         k = f"m{i}"
         mv.insert_model(k, S.synth_scene(n, seed=2 + i, translate_fraction=0.1))
         q = rng.normal(size=4)
         q /= np.linalg.norm(q)
         mv.update_model_transform(k, tuple(rng.normal(0.0, 0.5, 3)), tuple(q), (1.0, 1.0, 1.0))
         keys.append(k)
+    return mv, keys
+
+
+def measure_multi_model(args, mv, keys, pods, stream):
+    """Multi-model draw order at scale: one view of the four configuration models, drawn in key
+    order (model k over models < k) through MultiModelViewer.render."""
+    import torch
+
+    import gs300
+
+    W, H = args.width, args.height
+    sh = stream.cuda_stream
     t = gs300.RenderTarget(W, H)
     for k in range(3):
         mv.update_camera_with_pod(pods[k])
@@ -330,8 +357,223 @@ def measure_multi_model(args, pods, stream):
     torch.cuda.synchronize()
     mv.synchronize(stream=sh)
     ms = e0.elapsed_time(e1) / reps
+    return {"models": list(BATCH_MODELS), "fps": 1000.0 / ms, "ms": ms}
+
+
+def measure_batched_config(args, mv, keys, stream):
+    """The batching configuration: 64 views per launch, each one of the four models seen from a
+    random orbit (radius 6-12) at a resolution drawn from {640x360, 1280x720, 1920x1080,
+    3840x2160}, rendered by one CUDA graph per batch shape (gs_batch_render) with launch choices
+    from the autotuner, against the plain path rendering the same 64 views one at a time
+    (MultiModelViewer.render of the view's model).  Frames of both paths are compared."""
+    import torch
+
+    import gs300
+    from gs300 import scene as S
+
+    sh = stream.cuda_stream
+    rng = np.random.default_rng(11)
+    V = args.config_views
+    views, shapes = [], []
+    for i in range(V):
+        key = keys[int(rng.integers(0, len(keys)))]
+        w, h = BATCH_RES[int(rng.integers(0, len(BATCH_RES)))]
+        pod = gs300.CameraPod.new(S.random_orbit_camera(rng), (w, h))
+        views.append((key, pod, gs300.RenderTarget(w, h)))
+        shapes.append((w, h))
+    pixels = sum(w * h for w, h in shapes)
+    batch = gs300.Batch(mv, keys)
+    tuning, _ = batch.autotune(views, reps=2)
+    batch.render(views, stream=sh)
+    batch.synchronize(stream=sh)
+    reps = max(3, args.steps // 10)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        batch.render(views, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch.synchronize(stream=sh)
+    batched_ms = e0.elapsed_time(e1) / reps
+    batched = [v[2].download() for v in views]
+    # the plain path: each view alone, one after another on the same stream
+    plain_t = {wh: gs300.RenderTarget(*wh) for wh in set(shapes)}
+
+    def plain_round():
+        for key, pod, tgt in views:
+            mv.update_camera_with_pod(pod)
+            mv.render(plain_t[(tgt.width, tgt.height)], [key], stream=sh)
+
+    plain_round()
+    mv.synchronize(stream=sh)
+    same = True
+    for (key, pod, tgt), got in zip(views, batched):
+        mv.update_camera_with_pod(pod)
+        t = plain_t[(tgt.width, tgt.height)]
+        mv.render(t, [key], stream=sh)
+        mv.synchronize(stream=sh)
+        same = same and bool(np.array_equal(t.download(), got))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        plain_round()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    mv.synchronize(stream=sh)
+    plain_ms = e0.elapsed_time(e1) / reps
+    batch.close()
+    return {
+        "views": V, "models": list(BATCH_MODELS), "resolutions": sorted({f"{w}x{h}" for w, h in shapes}),
+        "views_per_resolution": {f"{w}x{h}": shapes.count((w, h)) for w, h in sorted(set(shapes))},
+        "batched_views_per_s": V / (batched_ms / 1000.0), "batched_ms_per_batch": batched_ms,
+        "batched_mpix_per_s": pixels / (batched_ms / 1000.0) / 1e6,
+        "plain_views_per_s": V / (plain_ms / 1000.0), "plain_ms_per_batch": plain_ms,
+        "speedup_vs_plain": plain_ms / batched_ms, "frames_identical": same, "tuning": tuning,
+    }
+
+
+def measure_served_config(args, stream):
+    """The serving configuration: 8 resident scenes of 0.5M-8M Gaussians (log-uniform counts, FP16
+    rotation/scale/SH records), requests picking a scene uniformly, a random orbit camera and a
+    resolution from {1280x720, 1920x1080, 3840x2160}.  First the closed-loop peak (all requests
+    queued at once), then open-loop Poisson arrivals at each offered rate of the sweep (and at 80%
+    of the peak), each over `--serve-requests` requests: completed frames/s and p50/p99
+    submit-to-done latency.  Beside it, the plain path: the same requests one at a time
+    (MultiModelViewer.render of the scene, waiting for each)."""
+    import torch
+
+    import gs300
+    from gs300 import records as R
+    from gs300 import scene as S
+
+    rng = np.random.default_rng(12)
+    counts = np.exp(rng.uniform(np.log(0.5e6), np.log(8e6), size=8)).astype(int)
+    mv = gs300.MultiModelViewer()
+    keys = []
+    for i, n in enumerate(counts):
+        k = f"s{i}"
+        mv.insert_model(k, S.synth_scene(int(n), seed=100 + i, fmt=R.FORMAT_HALF_SH_FP16), fmt=R.FORMAT_HALF_SH_FP16)
+        keys.append(k)
+    n_req = args.serve_requests
+
+    def requests(seed, count):
+        r = np.random.default_rng(seed)
+        out = []
+        for _ in range(count):
+            key = keys[int(r.integers(0, len(keys)))]
+            w, h = SERVE_RES[int(r.integers(0, len(SERVE_RES)))]
+            out.append((key, gs300.CameraPod.new(S.random_orbit_camera(r), (w, h)), w, h))
+        return out
+
+    inflight = args.serve_inflight
+    need = max(gs300.Server.request_bytes(int(n), w, h) for n in counts for w, h in SERVE_RES)
+    sv = gs300.Server(mv, budget_bytes=need * inflight, max_inflight=inflight)
+    sv.set_batching(16, max_wait_ms=args.serve_wait_ms)
+    # warm-up: every slot meets the largest scene at 4K, so its buffers reach their final sizes
+    big = keys[int(np.argmax(counts))]
+    for _ in range(2):
+        pod = gs300.CameraPod.new(S.orbit_camera(0), SERVE_RES[-1])
+        for t in [sv.submit(big, pod, *SERVE_RES[-1]) for _ in range(inflight)]:
+            sv.wait(t)
+    for key, pod, w, h in requests(1, 2 * inflight):
+        sv.wait(sv.submit(key, pod, w, h))
+    sv.reset_stats()
+    reqs = requests(2, n_req)
+    t0 = time.perf_counter()
+    for t in [sv.submit(key, pod, w, h) for key, pod, w, h in reqs]:
+        sv.wait(t)
+    peak = n_req / (time.perf_counter() - t0)
+    st = sv.stats()
+    closed = {"fps": peak, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"]}
+    sweep = []
+    rates = sorted(set([float(r) for r in args.serve_rates] + [round(0.8 * peak, 1)]))
+    for i, rate in enumerate(rates):
+        sv.reset_stats()
+        reqs = requests(10 + i, n_req)
+        arrivals = np.cumsum(np.random.default_rng(20 + i).exponential(1.0 / rate, size=n_req))
+        tickets = []
+        t0 = time.perf_counter()
+        for (key, pod, w, h), at in zip(reqs, arrivals):
+            dt = at - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            tickets.append(sv.submit(key, pod, w, h))
+        for t in tickets:
+            sv.wait(t)
+        elapsed = time.perf_counter() - t0
+        st = sv.stats()
+        sweep.append({"offered_rps": rate, "fps": n_req / elapsed, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                      "max_ms": st["max_ms"], "failed": st["failed"], "at_80pct_of_peak": rate == round(0.8 * peak, 1)})
+    sv.close()
+    # the plain path: the same kind of requests one at a time, each waited for
+    targets = {wh: gs300.RenderTarget(*wh) for wh in SERVE_RES}
+    plain_reqs = requests(3, max(50, n_req // 4))
+    sh = stream.cuda_stream
+    for key, pod, w, h in plain_reqs[:5]:
+        mv.update_camera_with_pod(pod)
+        mv.render(targets[(w, h)], [key], stream=sh)
+        mv.synchronize(stream=sh)
+    lat = []
+    t0 = time.perf_counter()
+    for key, pod, w, h in plain_reqs:
+        s0 = time.perf_counter()
+        mv.update_camera_with_pod(pod)
+        mv.render(targets[(w, h)], [key], stream=sh)
+        mv.synchronize(stream=sh)
+        lat.append(1000.0 * (time.perf_counter() - s0))
+    plain_fps = len(plain_reqs) / (time.perf_counter() - t0)
+    lat.sort()
     mv.close()
-    return {"models": [500_000, 1_000_000, 1_500_000, 3_000_000], "fps": 1000.0 / ms, "ms": ms}
+    torch.cuda.synchronize()
+    at80 = [r for r in sweep if r["at_80pct_of_peak"]][0]
+    return {
+        "scenes": [int(n) for n in counts], "format": "FP16 rotation/scale/SH (128-byte records)",
+        "resolutions": [f"{w}x{h}" for w, h in SERVE_RES], "requests_per_rate": n_req, "max_inflight": inflight,
+        "batch_wait_ms": args.serve_wait_ms, "closed_loop_peak": closed, "sweep": sweep,
+        "p99_ms_at_80pct_of_peak": at80["p99_ms"], "fps_at_80pct_of_peak": at80["fps"],
+        "plain_one_at_a_time": {"fps": plain_fps, "p50_ms": lat[len(lat) // 2],
+                                "p99_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))], "requests": len(plain_reqs)},
+        "peak_vs_plain": peak / plain_fps,
+    }
+
+
+def measure_precision_sample(args, scenes, pods_of):
+    """Frames of the plain path against the host FP64 oracle of the same pipeline on the same
+    pods and records, for FP32 records and for the FP16 rotation/scale + BF16 SH records of the
+    precision tier, over `--precision-sample-cameras` orbit cameras (the full 32-camera report is
+    `bench.py --precision`)."""
+    import gs300
+    from gs300 import records as R
+    from oracle import oracle as O
+
+    W, H, K = args.width, args.height, args.precision_sample_cameras
+    threads = os.cpu_count() or 1
+    out = {"cameras": [int(k * 120 / K) for k in range(K)], "oracle": "oracle/gs_oracle64.cpp (FP64)",
+           "oracle_threads": threads}
+    for name, fmt in (("fp32", R.FORMAT_FP32), ("half_sh_bf16", R.FORMAT_HALF_SH_BF16)):
+        sc = scenes[fmt]
+        v = gs300.Viewer(sc, fmt=None if fmt == R.FORMAT_FP32 else fmt)
+        t = gs300.RenderTarget(W, H)
+        psnr, maxerr, within1 = [], [], []
+        t0 = time.perf_counter()
+        for k in out["cameras"]:
+            pod = pods_of(k)
+            v.update_camera_with_pod(pod)
+            v.render(t)
+            v.synchronize()
+            got = t.download()
+            ref, _ = O.render64(pod, gs300.model_transform_pod(), gs300.gaussian_transform_pod(), sc, fmt, W, H,
+                                threads=threads)
+            d = got[..., :3].astype(np.int32) - ref[..., :3].astype(np.int32)
+            mse = float((d.astype(np.float64) ** 2).mean())
+            psnr.append(math.inf if mse == 0 else 10.0 * math.log10(255.0 ** 2 / mse))
+            maxerr.append(int(np.abs(d).max()))
+            within1.append(float((np.abs(d).max(axis=-1) <= 1).mean()))
+        v.close()
+        out[name] = {"psnr_db_min": min(psnr), "psnr_db_mean": statistics.mean(psnr), "max_err_max": max(maxerr),
+                     "within_1_min": min(within1), "seconds": time.perf_counter() - t0}
+    return out
 
 
 def measure_ply_ingest(args):

@@ -134,6 +134,14 @@ struct DevBuf {
         if (e == cudaSuccess) bytes = b;
         return e;
     }
+    // A scratch area: grown when too small, zero-filled only when (re)allocated — a reused area
+    // needs no clearing whatever sizes its next calls use (fixed-offset flag arena).
+    cudaError_t ensure_zeroed(size_t b) {
+        if (b <= bytes && ptr) return cudaSuccess;
+        cudaError_t e = ensure(b);
+        if (e == cudaSuccess) e = cudaMemset(ptr, 0, bytes);
+        return e;
+    }
 };
 
 gs_status status_from_bits(uint32_t bits, const char *what) {
@@ -260,13 +268,14 @@ struct Frame {
         gt.max_std_dev = 3.0f;
     }
 
+    // Raster scratch for `splats` splats at w x h.  It only grows: a frame at a smaller size is
+    // laid out inside the larger area (its flag arena sits at a fixed offset and is cleared on
+    // the device where a layout grows), so changing resolution or models allocates nothing once
+    // the largest frame has been seen.
     gs_status ensure_scratch(uint32_t splats, uint32_t w, uint32_t h) {
-        if (max_pairs == 0) max_pairs = default_pairs(splats, w, h);
-        if (raster_scratch.ptr && splats <= scratch_splats && w == scratch_w && h == scratch_h) return GS_OK;
-        const size_t b = raster_scratch_bytes(splats, w, h, max_pairs);
-        raster_scratch.release();
-        GS_CUDA(raster_scratch.ensure(b));
-        GS_CUDA(cudaMemset(raster_scratch.ptr, 0, b));
+        const uint32_t want = default_pairs(splats, w, h);
+        if (want > max_pairs) max_pairs = want;
+        GS_CUDA(raster_scratch.ensure_zeroed(raster_scratch_bytes(splats, w, h, max_pairs)));
         scratch_splats = splats;
         scratch_w = w;
         scratch_h = h;
@@ -1040,35 +1049,32 @@ struct ViewSlot {
     const Model *model = nullptr;
     uint32_t w = 0, h = 0;
     DevBuf control, indices, depths, splats, pre_scratch, sort_scratch, raster_scratch;
-    uint32_t max_pairs = 0, raster_n = 0, raster_w = 0, raster_h = 0;
+    uint32_t max_pairs = 0;
 
-    // Buffers of one view of `m` at w x h; returns true when anything was (re)allocated.
+    // Buffers of one view of `m` at w x h; *changed is set when any pointer changed (a captured
+    // graph must then be rebuilt).  Buffers only grow: a slot that served a larger scene or
+    // resolution keeps its buffers and lays the smaller view out inside them, so a mix of scenes
+    // and resolutions stops allocating once each slot has met its largest request.  The tile-pair
+    // capacity never shrinks either (it also keeps any growth after an overflow).
     cudaError_t prepare(const Model *m, uint32_t ww, uint32_t hh, bool *changed) {
         const uint32_t n = m->n;
         cudaError_t e = cudaSuccess;
-        if (model == nullptr || model->n != n) {
-            if ((e = control.ensure(64)) != cudaSuccess) return e;
-            if ((e = cudaMemset(control.ptr, 0, 64)) != cudaSuccess) return e;
-            if ((e = indices.ensure((size_t)n * 4)) != cudaSuccess) return e;
-            if ((e = depths.ensure((size_t)gs_depth_capacity(n) * 4)) != cudaSuccess) return e;
-            if ((e = splats.ensure((size_t)n * sizeof(gs_splat))) != cudaSuccess) return e;
-            if ((e = pre_scratch.ensure(preprocess_scratch_bytes(n))) != cudaSuccess) return e;
-            if ((e = cudaMemset(pre_scratch.ptr, 0, pre_scratch.bytes)) != cudaSuccess) return e;
-            if ((e = sort_scratch.ensure(sort_scratch_bytes(n, 32))) != cudaSuccess) return e;
-            if ((e = cudaMemset(sort_scratch.ptr, 0, sort_scratch.bytes)) != cudaSuccess) return e;
-            *changed = true;
-        }
-        if (max_pairs == 0) max_pairs = default_pairs(n, ww, hh);
-        if (!raster_scratch.ptr || raster_n < n || raster_w != ww || raster_h != hh) {
-            const size_t b = raster_scratch_bytes(n, ww, hh, max_pairs);
-            raster_scratch.release();
-            if ((e = raster_scratch.ensure(b)) != cudaSuccess) return e;
-            if ((e = cudaMemset(raster_scratch.ptr, 0, b)) != cudaSuccess) return e;
-            raster_n = n;
-            raster_w = ww;
-            raster_h = hh;
-            *changed = true;
-        }
+        const void *before[7] = {control.ptr, indices.ptr, depths.ptr, splats.ptr, pre_scratch.ptr, sort_scratch.ptr,
+                                 raster_scratch.ptr};
+        if ((e = control.ensure_zeroed(64)) != cudaSuccess) return e;
+        if ((e = indices.ensure((size_t)n * 4)) != cudaSuccess) return e;
+        if ((e = depths.ensure((size_t)gs_depth_capacity(n) * 4)) != cudaSuccess) return e;
+        if ((e = splats.ensure((size_t)n * sizeof(gs_splat))) != cudaSuccess) return e;
+        if ((e = pre_scratch.ensure_zeroed(preprocess_scratch_bytes(n))) != cudaSuccess) return e;
+        if ((e = sort_scratch.ensure_zeroed(sort_scratch_bytes(n, 32))) != cudaSuccess) return e;
+        const uint32_t want = default_pairs(n, ww, hh);
+        if (want > max_pairs) max_pairs = want;
+        if ((e = raster_scratch.ensure_zeroed(raster_scratch_bytes(n, ww, hh, max_pairs))) != cudaSuccess) return e;
+        const void *after[7] = {control.ptr, indices.ptr, depths.ptr, splats.ptr, pre_scratch.ptr, sort_scratch.ptr,
+                                raster_scratch.ptr};
+        for (int i = 0; i < 7; ++i)
+            if (before[i] != after[i]) *changed = true;
+        if (model != m || w != ww || h != hh) *changed = true;
         model = m;
         w = ww;
         h = hh;

@@ -156,6 +156,17 @@ def orbit_camera(k, radius=8.0, frames=120, pitch=0.1, yaw0=0.1, fovy_deg=60.0, 
     return Camera.new(z_near, z_far, math.radians(fovy_deg), pos=tuple(float(v) for v in pos), pitch=pitch, yaw=yaw)
 
 
+def random_orbit_camera(rng, radius_lo=6.0, radius_hi=12.0, pitch_max=0.3):
+    """A camera on a random orbit around the origin: radius uniform in [radius_lo, radius_hi], yaw
+    uniform, pitch uniform in [-pitch_max, pitch_max] (fovy 60°, z 0.1..1e4), looking at the origin."""
+    radius = float(rng.uniform(radius_lo, radius_hi))
+    yaw = float(rng.uniform(0.0, 2.0 * math.pi))
+    pitch = float(rng.uniform(-pitch_max, pitch_max))
+    fwd = np.array([math.cos(pitch) * math.sin(yaw), math.sin(pitch), math.cos(pitch) * math.cos(yaw)])
+    pos = -radius * fwd
+    return Camera.new(0.1, 1e4, math.radians(60.0), pos=tuple(float(v) for v in pos), pitch=pitch, yaw=yaw)
+
+
 def given_camera():
     """The reference tests' camera: yaw 0.1, pitch 0.1, z 0.1..1e4, fovy 60° (tests/common/given.rs:6-12)."""
     return Camera.new(0.1, 1e4, math.radians(60.0), pos=(0.0, 0.0, 0.0), pitch=0.1, yaw=0.1)
