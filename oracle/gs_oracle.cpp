@@ -604,6 +604,130 @@ void look_to_rh(const float eye[3], const float dir_in[3], const float up[3], fl
     out[15] = 1.0f;
 }
 
+// ------------------------------------------------------------------------------------------
+// The reference's vertex stage taken literally (render.wesl:46-56, 75-130), for checking the
+// pixel -> quad-offset map that preprocess_one hands the rasterisers: six clip-space vertices
+// per instance, proj·(view·(model·pos)) plus the quad corner offsets scaled by w (splat and
+// ellipse: along the std-scaled 2D axes; point: the point-size square, aspect H/W, divided by
+// |view_pos|); two triangles (vertices 0-2 and 3-5) rasterised at pixel centres under the
+// top-left fill rule; quad_offset interpolated at the pixel centre (the six vertices share w,
+// so linear interpolation in screen space is the perspective-correct one); frag_main
+// (render.wesl:143-181) in FP32; the blend of `blend`.  Screen positions and barycentrics are
+// FP64 (hardware snaps to a sub-pixel grid instead), everything the shaders compute is FP32.
+// ------------------------------------------------------------------------------------------
+struct QuadVert {
+    double x, y;  // screen position (pixels, y down)
+    float qx, qy; // quad_offset
+};
+
+void raster_triangle(QuadVert v0, QuadVert v1, QuadVert v2, uint32_t mode, float std_dev, float alpha_in,
+                     const gs_splat &colour, uint8_t *rgba, uint32_t W, uint32_t H) {
+    double area = (v1.x - v0.x) * (v2.y - v0.y) - (v1.y - v0.y) * (v2.x - v0.x);
+    if (!(std::isfinite(area) && area != 0.0)) return;
+    if (area < 0.0) {
+        std::swap(v1, v2);
+        area = -area;
+    }
+    const QuadVert v[3] = {v0, v1, v2};
+    const double xmin = std::min(v0.x, std::min(v1.x, v2.x)), xmax = std::max(v0.x, std::max(v1.x, v2.x));
+    const double ymin = std::min(v0.y, std::min(v1.y, v2.y)), ymax = std::max(v0.y, std::max(v1.y, v2.y));
+    const double x0 = std::max(0.0, std::floor(xmin - 1.0)), x1 = std::min((double)W - 1.0, std::ceil(xmax + 1.0));
+    const double y0 = std::max(0.0, std::floor(ymin - 1.0)), y1 = std::min((double)H - 1.0, std::ceil(ymax + 1.0));
+    if (!(x0 <= x1 && y0 <= y1)) return;
+    // With area > 0 in y-down screen space the triangle is clockwise on screen: an edge going
+    // up is a left edge, a horizontal edge going right is a top edge.
+    bool topleft[3];
+    for (int e = 0; e < 3; ++e) {
+        const QuadVert &a = v[e], &b = v[(e + 1) % 3];
+        topleft[e] = (a.y == b.y && b.x > a.x) || (b.y < a.y);
+    }
+    const float std2 = std_dev * std_dev;
+    const float o = std_dev - 0.1f;
+    const float outline2 = o * o;
+    for (uint32_t py = (uint32_t)y0; py <= (uint32_t)y1; ++py)
+        for (uint32_t px = (uint32_t)x0; px <= (uint32_t)x1; ++px) {
+            const double cx = (double)px + 0.5, cy = (double)py + 0.5;
+            double w[3];
+            bool in = true;
+            for (int e = 0; e < 3 && in; ++e) {
+                const QuadVert &a = v[e], &b = v[(e + 1) % 3];
+                w[e] = (b.x - a.x) * (cy - a.y) - (b.y - a.y) * (cx - a.x);
+                in = w[e] > 0.0 || (w[e] == 0.0 && topleft[e]);
+            }
+            if (!in) continue;
+            // edge e lies opposite vertex (e + 2) % 3
+            const double l0 = w[1] / area, l1 = w[2] / area, l2 = w[0] / area;
+            const float qx = (float)(l0 * v[0].qx + l1 * v[1].qx + l2 * v[2].qx);
+            const float qy = (float)(l0 * v[0].qy + l1 * v[1].qy + l2 * v[2].qy);
+            float alpha;
+            if (mode == GS_DISPLAY_POINT) {
+                alpha = 1.0f;
+            } else {
+                const float r2 = qx * qx + qy * qy;  // dot(in.quad_offset, in.quad_offset)
+                if (r2 > std2) continue;             // discard
+                if (mode == GS_DISPLAY_SPLAT) {
+                    alpha = alpha_in * std::exp(-r2);
+                } else {
+                    const bool outline = r2 > outline2;
+                    alpha = alpha_in + (1.0f - alpha_in) * (outline ? 1.0f : 0.0f);
+                }
+            }
+            blend(rgba + ((size_t)py * W + px) * 4, colour, alpha);
+        }
+}
+
+// vert_main for the six vertices of one instance, then its two triangles.
+void draw_instance(const gs_frame_uniforms &u, const gs_camera_pod &cam, const Record &g, uint8_t *rgba, uint32_t W,
+                   uint32_t H) {
+    static const float corner[6][2] = {{1.0f, -1.0f}, {-1.0f, -1.0f}, {1.0f, 1.0f},
+                                       {-1.0f, 1.0f}, {1.0f, 1.0f}, {-1.0f, -1.0f}};
+    const float p4[4] = {g.pos[0], g.pos[1], g.pos[2], 1.0f};
+    float world[4], view_pos[4], proj_pos[4];
+    mat4_vec(u.model, p4, world);
+    mat4_vec(cam.view, world, view_pos);
+    mat4_vec(cam.proj, view_pos, proj_pos);
+    float rgba_f[4];
+    view_color(u, g, world, rgba_f);
+    gs_splat colour{};
+    colour.s255[0] = clamp01(rgba_f[0]) * 255.0f;  // a Rgba8Unorm attachment clamps the source
+    colour.s255[1] = clamp01(rgba_f[1]) * 255.0f;
+    colour.s255[2] = clamp01(rgba_f[2]) * 255.0f;
+    const float w = proj_pos[3];
+    // depth clipping: z / w outside [0, 1] (all vertices share z and w)
+    if (!(proj_pos[2] >= 0.0f && proj_pos[2] <= w)) return;
+    float clip[6][2], q[6][2];
+    if (u.display_mode == GS_DISPLAY_POINT) {
+        const float aspect = u.size[1] / u.size[0];  // camera_aspect_ratio = size.y / size.x
+        const float len = std::sqrt((view_pos[0] * view_pos[0] + view_pos[1] * view_pos[1]) + view_pos[2] * view_pos[2]);
+        for (int k = 0; k < 6; ++k) {
+            q[k][0] = (corner[k][0] * 0.01f) * u.point_size;
+            q[k][1] = (corner[k][1] * 0.01f) * u.point_size;
+            clip[k][0] = proj_pos[0] + ((q[k][0] * w) * aspect) / len;
+            clip[k][1] = proj_pos[1] + ((q[k][1] * w) * 1.0f) / len;
+        }
+    } else {
+        float axes[4];
+        cov2d_axes(u, g, p4, u.std_dev_scaled, axes);
+        if (axes[0] == 0.0f && axes[1] == 0.0f && axes[2] == 0.0f && axes[3] == 0.0f) return;  // clip z = 2
+        for (int k = 0; k < 6; ++k) {
+            q[k][0] = corner[k][0] * u.std_dev;
+            q[k][1] = corner[k][1] * u.std_dev;
+            clip[k][0] = (proj_pos[0] + ((q[k][0] * w) * axes[0]) / u.size[0]) + ((q[k][1] * w) * axes[2]) / u.size[0];
+            clip[k][1] = (proj_pos[1] + ((q[k][0] * w) * axes[1]) / u.size[1]) + ((q[k][1] * w) * axes[3]) / u.size[1];
+        }
+    }
+    QuadVert vs[6];
+    for (int k = 0; k < 6; ++k) {
+        const double nx = (double)clip[k][0] / (double)w, ny = (double)clip[k][1] / (double)w;
+        vs[k].x = (nx + 1.0) * 0.5 * (double)W;
+        vs[k].y = (1.0 - ny) * 0.5 * (double)H;
+        vs[k].qx = q[k][0];
+        vs[k].qy = q[k][1];
+    }
+    raster_triangle(vs[0], vs[1], vs[2], u.display_mode, u.std_dev, rgba_f[3], colour, rgba, W, H);
+    raster_triangle(vs[3], vs[4], vs[5], u.display_mode, u.std_dev, rgba_f[3], colour, rgba, W, H);
+}
+
 }  // namespace
 
 extern "C" {
@@ -779,6 +903,19 @@ void oracle_rasterize(const gs_frame_uniforms *u, const gs_splat *splats, const 
 }
 
 float oracle_exp_portable(float x) { return exp_portable(x); }
+
+// The frame through the reference's own vertex stage (draw_instance): the same preprocess,
+// stable depth sort and cleared target, then every visible instance's two triangles in draw
+// order.  Single-threaded; a parity check of the quad map, sized for small frames.  Returns V.
+uint32_t oracle_render_quads(const gs_camera_pod *cam, const gs_frame_uniforms *u, const void *gaussians,
+                             uint32_t format, uint32_t n, uint32_t *indices, float *depths, uint8_t *rgba,
+                             uint32_t w, uint32_t h, int clear) {
+    const uint32_t v = oracle_preprocess(u, gaussians, format, n, nullptr, 0, indices, depths, nullptr, 1);
+    oracle_stable_sort((uint32_t *)depths, indices, v);
+    if (clear) oracle_clear(rgba, w, h);
+    for (uint32_t k = 0; k < v; ++k) draw_instance(*u, *cam, load_record(gaussians, format, indices[k]), rgba, w, h);
+    return v;
+}
 
 // Full frame: preprocess -> stable sort -> clear -> raster.  Scratch arrays are caller-sized
 // (indices/depths: n; splats: n).  Returns V.

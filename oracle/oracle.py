@@ -41,6 +41,8 @@ def _declare(L):
     L.oracle64_render.argtypes = [P, P, P, P, U, U, P, U, U, I]
     L.oracle64_render.restype = U
     L.oracle_ply_convert.argtypes = [P, P, U, P]
+    L.oracle_render_quads.argtypes = [P, P, P, U, U, P, P, P, U, U, I]
+    L.oracle_render_quads.restype = U
     L.oracle_wgpu_radix_sort.argtypes = [P, U, P, U, U, U, I]
     L.oracle_wgpu_radix_sort.restype = I
 
@@ -163,3 +165,17 @@ def wgpu_radix_sort(keys, payload, num_keys, dispatch_x, schedule=0):
     if rc != 0:
         raise RuntimeError("reference sorter restatement: a look-back met an unpublished predecessor")
     return k, p
+
+
+def render_quads(camera_pod, u, records, fmt, w, h, target=None):
+    """The frame through the reference's own vertex stage taken literally (six clip-space
+    vertices per instance, two triangles rasterised at pixel centres, interpolated quad offsets,
+    frag_main): the check of the pixel -> quad map every other rasteriser here shares.
+    Returns (rgba, V)."""
+    n = len(records)
+    idx = np.zeros(max(n, 1), np.uint32)
+    dep = np.zeros(max(n, 1), np.float32)
+    img = target if target is not None else np.empty((h, w, 4), np.uint8)
+    v = lib().oracle_render_quads(_p(camera_pod), _p(u), _p(records), fmt, n, _p(idx), _p(dep), _p(img), w, h,
+                                  0 if target is not None else 1)
+    return img, v

@@ -156,3 +156,25 @@ def test_profile_modes_render_the_same_frame(gs, cuda):
         gs.profile_enable(False)
     assert np.array_equal(plain, timed) and np.array_equal(plain, counted)
     assert c["evaluations"] >= c["alphas"] > 0 and c["blends"] > 0
+
+
+@pytest.mark.parametrize("mode", [R.DISPLAY_SPLAT, R.DISPLAY_ELLIPSE, R.DISPLAY_POINT])
+def test_frames_against_the_reference_vertex_stage(gs, cuda, oracle, mode):
+    """The CUDA frame (default SFU exp) against the oracle that runs the reference's vertex stage
+    literally (six clip-space vertices per instance, two triangles, interpolated quad offset):
+    at least 99.9 % of pixels within 1/255 and PSNR >= 45 dB."""
+    n, w, h = 100_000, 640, 360
+    sc = S.synth_scene(n, seed=77)
+    v = gs.Viewer(sc)
+    v.update_gaussian_transform(1.0, mode, 3, False, 3.0)
+    cam = S.orbit_camera(17, radius=7.0)
+    v.update_camera(cam, (w, h))
+    t = gs.RenderTarget(w, h)
+    v.render(t)
+    v.synchronize()
+    got = t.download()
+    pod = gs.CameraPod.new(cam, (w, h))
+    u = oracle.frame_uniforms(pod, gs.model_transform_pod(), gs.gaussian_transform_pod(display_mode=mode), w, h)
+    want, vis = oracle.render_quads(pod, u, sc, R.FORMAT_FP32, w, h)
+    assert vis > 0
+    assert within_one_fraction(got, want) >= 0.999 and frame_psnr(got, want) >= 45.0
