@@ -376,8 +376,12 @@ typedef struct gs_tuning {
     uint32_t hist_blocks;      /* depth sort key-histogram blocks, 0 (by key count) or 1..1216 */
     uint32_t raster_grid;      /* 0: each view rasterised after its own binning (overlapping other
                                   views' sorting); 1: one rasteriser grid over all views' tiles */
+    uint32_t sort_digit_bits;  /* depth sort: widest radix digit of a pass, 6..8 (the key's bits
+                                  spread evenly over the passes): narrower digits give longer
+                                  runs of equal digits per block at the price of more passes */
 } gs_tuning;
-/* The library's defaults (GS300_SUFFIX_MIN / GS300_SUFFIX_EPS override the raster knobs). */
+/* The library's defaults (GS300_SUFFIX_MIN / GS300_SUFFIX_EPS override the raster knobs,
+ * GS300_SORT_DIGIT_BITS the depth sort's digit width). */
 gs_status gs_tuning_default(gs_tuning *out);
 /* GS_ERR_INVALID_ARG outside the ranges above.  The next render re-captures the graph. */
 gs_status gs_batch_set_tuning(gs_batch *batch, const gs_tuning *tuning);

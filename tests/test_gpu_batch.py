@@ -99,11 +99,13 @@ TUNINGS = [
     dict(sort_match=0, hist_blocks=7, views_per_launch=3, streams=5),
     dict(raster_grid=1),                    # one rasteriser grid over all views
     dict(raster_grid=1, views_per_launch=2, streams=3, suffix_min=1),
+    dict(sort_digit_bits=6),                # six depth-sort passes of 5 and 6 bits
+    dict(sort_digit_bits=7, sort_match=0),  # five passes of 6 bits, ballot ranking
 ]
 
 
 @pytest.mark.parametrize("knobs", TUNINGS, ids=["serial", "early_out_everywhere", "ballot_sort", "one_grid",
-                                                "one_grid_early_out"])
+                                                "one_grid_early_out", "digits_6", "digits_7_ballot"])
 def test_batch_tuning_changes_no_frame(gs, cuda, monkeypatch, knobs):
     monkeypatch.setenv("GS300_EXACT_EXP", "1")
     sc = S.synth_scene(40_000, seed=12)
@@ -128,7 +130,7 @@ def test_batch_tuning_rejects_bad_values(gs, cuda):
     batch = gs.Batch(mv, ["m"])
     for bad in (dict(views_per_launch=0), dict(views_per_launch=17), dict(streams=0), dict(streams=17),
                 dict(sort_match=2), dict(eps=0.0), dict(eps=0.7), dict(suffix_min=0), dict(hist_blocks=5000),
-                dict(raster_grid=2)):
+                dict(raster_grid=2), dict(sort_digit_bits=5), dict(sort_digit_bits=9)):
         with pytest.raises(gs.GsError):
             batch.set_tuning(**bad)
     assert batch.tuning == gs.tuning_default()

@@ -211,7 +211,7 @@ struct Model {
         GS_CUDA(splats.ensure((size_t)n * sizeof(gs_splat)));
         GS_CUDA(pre_scratch.ensure(preprocess_scratch_bytes(n)));
         GS_CUDA(cudaMemset(pre_scratch.ptr, 0, pre_scratch.bytes));
-        GS_CUDA(sort_scratch.ensure(sort_scratch_bytes(n, 32)));
+        GS_CUDA(sort_scratch.ensure(sort_scratch_bytes(n, kDepthKeyBits)));
         GS_CUDA(cudaMemset(sort_scratch.ptr, 0, sort_scratch.bytes));
         return GS_OK;
     }
@@ -223,7 +223,8 @@ struct Model {
                                           indirect(), indirect() + 4, (uint32_t *)indices.ptr, (float *)depths.ptr,
                                           gs_depth_capacity(n), (gs_splat *)splats.ptr, pre_scratch.ptr, st);
         if (e != cudaSuccess) return cuda_fail(e, "preprocess launch");
-        e = launch_sort((uint32_t *)depths.ptr, (uint32_t *)indices.ptr, n, indirect() + 1, 32, sort_scratch.ptr, st);
+        e = launch_sort((uint32_t *)depths.ptr, (uint32_t *)indices.ptr, n, indirect() + 1, kDepthKeyBits,
+                        sort_scratch.ptr, st);
         if (e != cudaSuccess) return cuda_fail(e, "sort launch");
         return GS_OK;
     }
@@ -1066,7 +1067,7 @@ struct ViewSlot {
         if ((e = depths.ensure((size_t)gs_depth_capacity(n) * 4)) != cudaSuccess) return e;
         if ((e = splats.ensure((size_t)n * sizeof(gs_splat))) != cudaSuccess) return e;
         if ((e = pre_scratch.ensure_zeroed(preprocess_scratch_bytes(n))) != cudaSuccess) return e;
-        if ((e = sort_scratch.ensure_zeroed(sort_scratch_bytes(n, 32))) != cudaSuccess) return e;
+        if ((e = sort_scratch.ensure_zeroed(sort_scratch_bytes(n, kDepthKeyBits))) != cudaSuccess) return e;
         const uint32_t want = default_pairs(n, ww, hh);
         if (want > max_pairs) max_pairs = want;
         if ((e = raster_scratch.ensure_zeroed(raster_scratch_bytes(n, ww, hh, max_pairs))) != cudaSuccess) return e;
@@ -1269,7 +1270,7 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
                 uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
                 if (vs != cs) err = cudaStreamWaitEvent(vs, b->chunk_events[c], 0);
                 if (err == cudaSuccess)
-                    err = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, ms[i]->n, ind + 1, 32,
+                    err = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, ms[i]->n, ind + 1, kDepthKeyBits,
                                       v.sort_scratch.ptr, vs, kProfDepthSort, &b->tuning);
                 if (err == cudaSuccess) {
                     const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1,
@@ -1392,6 +1393,7 @@ gs_tuning to_public(const gs::Tuning &t) {
     o.views_per_launch = t.views_per_launch;
     o.streams = t.streams;
     o.sort_match = t.sort_match;
+    o.sort_digit_bits = t.sort_digit_bits;
     o.hist_blocks = t.hist_blocks;
     o.raster_grid = t.raster_grid;
     return o;
@@ -1406,6 +1408,8 @@ gs_status from_public(const gs_tuning *p, gs::Tuning *t) {
     if (p->streams < 1 || p->streams > kBatchStreams)
         return fail(GS_ERR_INVALID_ARG, "streams %u outside 1..%u", p->streams, kBatchStreams);
     if (p->sort_match > 1) return fail(GS_ERR_INVALID_ARG, "sort_match must be 0 or 1");
+    if (p->sort_digit_bits < 6 || p->sort_digit_bits > 8)
+        return fail(GS_ERR_INVALID_ARG, "sort_digit_bits %u outside 6..8", p->sort_digit_bits);
     if (p->hist_blocks > 152 * 8) return fail(GS_ERR_INVALID_ARG, "hist_blocks %u above 1216", p->hist_blocks);
     if (p->raster_grid > 1) return fail(GS_ERR_INVALID_ARG, "raster_grid must be 0 or 1");
     t->suffix_min = p->suffix_min;
@@ -1413,6 +1417,7 @@ gs_status from_public(const gs_tuning *p, gs::Tuning *t) {
     t->views_per_launch = p->views_per_launch;
     t->streams = p->streams;
     t->sort_match = p->sort_match;
+    t->sort_digit_bits = p->sort_digit_bits;
     t->hist_blocks = p->hist_blocks;
     t->raster_grid = p->raster_grid;
     return GS_OK;
@@ -1510,15 +1515,17 @@ gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n,
     const uint32_t streams_c[] = {4, 8, 16};
     const uint32_t match_c[] = {0, 1};
     const uint32_t hist_c[] = {0, 304, 608};
+    const uint32_t digit_c[] = {6, 7, 8};
     const uint32_t grid_c[] = {0, 1};
     for (uint32_t round = 0; round < rounds && s == GS_OK; ++round) {
-        for (int knob = 0; knob < 7 && s == GS_OK; ++knob) {
+        for (int knob = 0; knob < 8 && s == GS_OK; ++knob) {
             const size_t nc = knob == 0   ? 4
                               : knob == 1 ? 2
                               : knob == 2 ? 4
                               : knob == 3 ? 3
                               : knob == 4 ? 2
                               : knob == 5 ? 3
+                              : knob == 6 ? 3
                                           : 2;
             for (size_t c = 0; c < nc && s == GS_OK; ++c) {
                 gs::Tuning t = best;
@@ -1529,10 +1536,12 @@ gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n,
                     case 3: t.streams = streams_c[c]; break;
                     case 4: t.sort_match = match_c[c]; break;
                     case 5: t.hist_blocks = hist_c[c]; break;
+                    case 6: t.sort_digit_bits = digit_c[c]; break;
                     default: t.raster_grid = grid_c[c]; break;
                 }
                 if (t.suffix_min == best.suffix_min && t.eps == best.eps && t.views_per_launch == best.views_per_launch &&
                     t.streams == best.streams && t.sort_match == best.sort_match && t.hist_blocks == best.hist_blocks &&
+                    t.sort_digit_bits == best.sort_digit_bits &&
                     t.raster_grid == best.raster_grid)
                     continue;
                 double ms = 0.0;
@@ -1567,7 +1576,7 @@ double now_ms() {
 // Device bytes one request holds while admitted: its key/index/splat buffers, scratch of the
 // three stages (tile-pair list at the default capacity) and its render target.
 size_t request_bytes(uint32_t n, uint32_t w, uint32_t h) {
-    return (size_t)n * (4 + 4 + sizeof(gs_splat)) + preprocess_scratch_bytes(n) + sort_scratch_bytes(n, 32) +
+    return (size_t)n * (4 + 4 + sizeof(gs_splat)) + preprocess_scratch_bytes(n) + sort_scratch_bytes(n, kDepthKeyBits) +
            raster_scratch_bytes(n, w, h, default_pairs(n, w, h)) + (size_t)w * h * 4;
 }
 
@@ -1665,7 +1674,7 @@ gs_status server_finish(gs_server *sv, ServerReq &r, ServerSlot &sl, uint8_t *ta
     const Model *m = r.model;
     ViewSlot &v = sl.view;
     uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
-    cudaError_t e = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, 32,
+    cudaError_t e = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, kDepthKeyBits,
                                 v.sort_scratch.ptr, sl.stream);
     if (e == cudaSuccess) {
         const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};

@@ -77,14 +77,22 @@ struct Tuning {
     uint32_t views_per_launch = 16; // batch: views per shared-read preprocess launch (1..16)
     uint32_t streams = 16;          // batch: streams the captured graph fans out over (1..16)
     uint32_t sort_match = 1;        // depth sort: 1 = match.any ranking, 0 = a ballot per digit bit
+    uint32_t sort_digit_bits = 8;   // depth sort: widest digit of a pass (6..8), bits spread evenly
     uint32_t hist_blocks = 0;       // depth sort: key-histogram grid (0 = by key count, <= 1216)
     uint32_t raster_grid = 0;       // batch: 0 = each view rasterised after its own binning,
                                     // 1 = one rasteriser grid over all views after all binning
 };
-// The defaults, with GS300_SUFFIX_MIN / GS300_SUFFIX_EPS / GS300_HIST_BLOCKS overriding them.
+// The defaults, with GS300_SUFFIX_MIN / GS300_SUFFIX_EPS / GS300_HIST_BLOCKS /
+// GS300_SORT_DIGIT_BITS overriding them.
 Tuning default_tuning();
 
 // ---- K2 onesweep radix sort (gs_sort.cu) ----
+// Live bits of a depth key: the key is 1 - ndc.z of a Gaussian whose ndc.z passed the cull test
+// (0 <= ndc.z <= 1, src/shader/utils.wesl:18-20), so it lies in [0, 1] and its float bits are at
+// most 0x3F800000 < 2^30.  Sorting bits [0, 30) orders every depth key exactly as sorting all 32.
+constexpr uint32_t kDepthKeyBits = 30;
+// Passes of a sort at most (32-bit keys in 6-bit digits).
+constexpr uint32_t kMaxPasses = 6;
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits);
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage = kProfDepthSort,
@@ -93,9 +101,15 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
 // Digits of the packed-pair sort: the key's bits spread evenly over the fewest passes of at
 // most 8 bits (13 bits -> 7 + 6), pass p taking bits [shift[p], shift[p] + bits[p]).
 struct PassSplit {
-    uint32_t shift[4], bits[4], n;
+    uint32_t shift[kMaxPasses], bits[kMaxPasses], n;
 };
 PassSplit even_split(uint32_t key_bits);
+// The same spread with digits of at most `max_digit` bits (6..8): fewer digit values per pass
+// mean longer runs of equal digits in each block's scatter, at the price of more passes.
+PassSplit even_split_max(uint32_t key_bits, uint32_t max_digit);
+// Offset of pass p's digit histogram in Ctrl::hist (flat): 256 words a pass for up to 4 passes,
+// 1024 / n words a pass beyond (enough for the narrower digits that more passes use).
+__host__ __device__ inline uint32_t hist_stride(uint32_t npasses) { return npasses <= 4 ? 256u : 1024u / npasses; }
 
 // Packed (uint2 {key, value}) in-place sort for internal pair lists whose digit histograms
 // (split by even_split) the producer accumulated into the control block `ctrl` after

@@ -129,6 +129,7 @@ Tuning default_tuning() {
     Tuning t;
     if (const char *v = getenv("GS300_SUFFIX_MIN")) t.suffix_min = (uint32_t)strtoul(v, nullptr, 10);
     if (const char *v = getenv("GS300_SUFFIX_EPS")) t.eps = strtof(v, nullptr);
+    if (const char *v = getenv("GS300_SORT_DIGIT_BITS")) t.sort_digit_bits = (uint32_t)strtoul(v, nullptr, 10);
     if (const char *v = getenv("GS300_HIST_BLOCKS")) t.hist_blocks = (uint32_t)strtoul(v, nullptr, 10);
     return t;
 }

@@ -63,15 +63,17 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, u
 // iteration, 16-byte loads when the keys are 16-byte aligned).  Per pass, the warp counts the
 // digit of lane 0 with one ballot (the high digits of float depth keys are nearly constant, and
 // same-address shared atomics would serialise) and the other keys with plain shared atomics.
-__device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool valid, uint32_t key_bits,
+__device__ __forceinline__ void hist_add(uint32_t *h, uint32_t k, bool valid, const PassSplit &sp, uint32_t hs,
                                          uint32_t lane) {
-    for (uint32_t p = 0; 8u * p < key_bits; ++p) {
-        const uint32_t left = key_bits - 8u * p;
-        const uint32_t d = (k >> (8u * p)) & ((left < 8u ? (1u << left) : 256u) - 1u);
+    // unrolled over the fixed maximum so every field of the split is read at a constant offset
+#pragma unroll
+    for (uint32_t p = 0; p < kMaxPasses; ++p) {
+        if (p >= sp.n) break;
+        const uint32_t d = (k >> sp.shift[p]) & ((1u << sp.bits[p]) - 1u);
         const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
         const uint32_t same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
-        if (lane == 0 && same) atomicAdd(&h[p][d0], (uint32_t)__popc(same));
-        if (valid && d != d0) atomicAdd(&h[p][d], 1u);
+        if (lane == 0 && same) atomicAdd(&h[p * hs + d0], (uint32_t)__popc(same));
+        if (valid && d != d0) atomicAdd(&h[p * hs + d], 1u);
     }
 }
 
@@ -79,11 +81,12 @@ __device__ __forceinline__ void hist_add(uint32_t (*h)[256], uint32_t k, bool va
 // which are the arena's only readers, run after this kernel).
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restrict__ keys,
                                                         const uint32_t *count, uint32_t max_count,
-                                                        uint32_t key_bits, Ctrl *ctrl, uint64_t *arena) {
-    __shared__ uint32_t h[4][256];
-    const uint32_t npasses = (key_bits + 7u) / 8u;
+                                                        const PassSplit sp, Ctrl *ctrl, uint64_t *arena) {
+    __shared__ uint32_t h[1024];
+    const uint32_t npasses = sp.n, hs = hist_stride(sp.n);
+    uint32_t *gh = &ctrl->hist[0][0];
     arena_clear(ctrl, arena);
-    for (uint32_t k = threadIdx.x; k < 4 * 256; k += blockDim.x) (&h[0][0])[k] = 0u;
+    for (uint32_t k = threadIdx.x; k < 1024; k += blockDim.x) h[k] = 0u;
     __syncthreads();
     const uint32_t n = load_count(count, max_count);
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -106,12 +109,12 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
             for (uint32_t j = 0; j < 4; ++j) k[j] = i0 + j < n ? keys[i0 + j] : 0u;
         }
 #pragma unroll
-        for (uint32_t j = 0; j < 4; ++j) hist_add(h, k[j], i0 + j < n, key_bits, lane);
+        for (uint32_t j = 0; j < 4; ++j) hist_add(h, k[j], i0 + j < n, sp, hs, lane);
     }
     __syncthreads();
     for (uint32_t p = 0; p < npasses; ++p) {
-        const uint32_t v = h[p][threadIdx.x];
-        if (v) atomicAdd(&ctrl->hist[p][threadIdx.x], v);
+        const uint32_t v = threadIdx.x < (1u << sp.bits[p]) ? h[p * hs + threadIdx.x] : 0u;
+        if (v) atomicAdd(&gh[p * hs + threadIdx.x], v);
     }
     // The last CTA to finish turns the histograms into exclusive digit offsets, once for every
     // block of every pass.
@@ -124,8 +127,9 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
         __threadfence();
         for (uint32_t p = 0; p < npasses; ++p) {
             uint32_t total;
-            const uint32_t off = block_scan_excl(__ldcg(&ctrl->hist[p][threadIdx.x]), s_tmp, &total);
-            ctrl->hist[p][threadIdx.x] = off;
+            const bool live = threadIdx.x < (1u << sp.bits[p]);
+            const uint32_t off = block_scan_excl(live ? __ldcg(&gh[p * hs + threadIdx.x]) : 0u, s_tmp, &total);
+            if (live) gh[p * hs + threadIdx.x] = off;
         }
     }
 }
@@ -178,7 +182,7 @@ template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
 __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
-    uint32_t max_count, uint32_t pass, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
+    uint32_t max_count, uint32_t hoff, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
     uint32_t hist_scanned) {
     __shared__ uint2 s_kv[kTileKeys];
     __shared__ uint32_t s_whist[kSortWarps][256];
@@ -268,7 +272,9 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     const uint32_t start = block_scan_excl(total, s_tmp, &blk_total);
     // the digit's first place in the output: the histograms hold exclusive offsets already
     // when their producer scanned them (hist_scanned is uniform over the grid)
-    const uint32_t goff = hist_scanned ? ctrl->hist[pass][d] : block_scan_excl(ctrl->hist[pass][d], s_tmp, &hist_total);
+    // (pass histogram at flat offset hoff; digits above dmask hold no key)
+    const uint32_t hv = live ? (&ctrl->hist[0][0])[hoff + d] : 0u;
+    const uint32_t goff = hist_scanned ? hv : block_scan_excl(hv, s_tmp, &hist_total);
     uint32_t prefix = 0;
     if (tile > 0 && live) {
         prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status, fstride, s_limit);
@@ -346,22 +352,23 @@ PassSplit even_split(uint32_t key_bits) {
     return sp;
 }
 
-static inline uint32_t pass_bits(uint32_t key_bits, uint32_t p) {
-    const uint32_t left = key_bits - 8u * p;
-    return left < 8u ? left : 8u;
-}
-
-// Passes of the split-array sort: 8-bit digits from bit 0, the last one narrower when key_bits
-// is not a multiple of 8.
-static PassSplit lsd_split(uint32_t key_bits) {
+// Passes of `key_bits` in digits of at most max_digit bits, spread evenly.
+PassSplit even_split_max(uint32_t key_bits, uint32_t max_digit) {
     PassSplit sp{};
-    sp.n = sort_passes(key_bits);
+    sp.n = (key_bits + max_digit - 1) / max_digit;
+    if (sp.n > kMaxPasses) sp.n = kMaxPasses;
+    const uint32_t base = sp.n ? key_bits / sp.n : 0u, extra = sp.n ? key_bits % sp.n : 0u;
+    uint32_t at = 0;
     for (uint32_t p = 0; p < sp.n; ++p) {
-        sp.shift[p] = 8u * p;
-        sp.bits[p] = pass_bits(key_bits, p);
+        sp.shift[p] = at;
+        sp.bits[p] = base + (p < extra ? 1u : 0u);
+        at += sp.bits[p];
     }
     return sp;
 }
+
+// Digit widths the split-array sort can be run with (Tuning::sort_digit_bits).
+constexpr uint32_t kMinDigitBits = 6, kMaxDigitBits = 8;
 
 static size_t sort_tiles(uint32_t max_count) {
     size_t t = (max_count + kTileKeys - 1) / kTileKeys;
@@ -401,10 +408,19 @@ static SortLayout sort_layout(void *scratch, uint32_t max_count, const PassSplit
     return L;
 }
 
+// Sized for the widest layout over every digit width a call may use, so a caller's scratch fits
+// whatever width the tuning picks.
 size_t sort_scratch_bytes(uint32_t max_count, uint32_t key_bits) {
-    const PassSplit sp = lsd_split(key_bits);
-    return align_up(sizeof(Ctrl), 256) + align_up(sort_flag_words(max_count, sp) * sizeof(uint64_t), 256) +
-           (sp.n >= 3 ? 2 : 1) * align_up((size_t)max_count * 8, 256);
+    size_t flags = 0;
+    uint32_t np = 0;
+    for (uint32_t db = kMinDigitBits; db <= kMaxDigitBits; ++db) {
+        const PassSplit sp = even_split_max(key_bits, db);
+        const size_t f = sort_flag_words(max_count, sp);
+        if (f > flags) flags = f;
+        if (sp.n > np) np = sp.n;
+    }
+    return align_up(sizeof(Ctrl), 256) + align_up(flags * sizeof(uint64_t), 256) +
+           (np >= 3 ? 2 : 1) * align_up((size_t)max_count * 8, 256);
 }
 
 static uint32_t grid_for(uint32_t max_count) {
@@ -416,7 +432,7 @@ static uint32_t grid_for(uint32_t max_count) {
 template <bool MATCH>
 static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                                const PassSplit &sp, const SortLayout &L, cudaStream_t st) {
-    const uint32_t npasses = sp.n;
+    const uint32_t npasses = sp.n, hs = hist_stride(sp.n);
     uint64_t *f = L.flags;
     if (npasses == 1) {
         sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
@@ -431,14 +447,15 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
     f += (size_t)L.ntiles << sp.bits[0];
     for (uint32_t p = 1; p + 1 < npasses; ++p) {
         sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p, sp.shift[p], sp.bits[p], L.ctrl, f, 1u);
+            nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p * hs, sp.shift[p], sp.bits[p], L.ctrl, f,
+            1u);
         f += (size_t)L.ntiles << sp.bits[p];
         uint2 *t = src;
         src = dst;
         dst = t;
     }
     sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
-        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, npasses - 1, sp.shift[npasses - 1],
+        nullptr, nullptr, src, keys, vals, nullptr, count, max_count, (npasses - 1) * hs, sp.shift[npasses - 1],
         sp.bits[npasses - 1], L.ctrl, f, 1u);
     count_launches(npasses);
 }
@@ -446,7 +463,10 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage, const Tuning *tuning) {
     const Tuning tn = tuning ? *tuning : default_tuning();
-    const PassSplit sp = lsd_split(key_bits);
+    const uint32_t db = tn.sort_digit_bits < kMinDigitBits   ? kMinDigitBits
+                        : tn.sort_digit_bits > kMaxDigitBits ? kMaxDigitBits
+                                                             : tn.sort_digit_bits;
+    const PassSplit sp = even_split_max(key_bits, db);
     const SortLayout L = sort_layout(scratch, max_count, sp);
     // With no pairs no kernel reads the flags, and none clears them: the arena mark stays.
     ctrl_init_kernel<<<1, 256, 0, st>>>(L.ctrl, 1, nullptr, max_count ? (uint32_t)L.flag_words : kKeepArena,
@@ -457,7 +477,7 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     uint32_t hist_blocks = (max_count + 256 * 4 * 4 - 1) / (256 * 4 * 4);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
     if (tn.hist_blocks) hist_blocks = tn.hist_blocks < 152 * 8 ? tn.hist_blocks : 152 * 8;
-    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, key_bits, L.ctrl, L.flags);
+    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, sp, L.ctrl, L.flags);
     count_launches(1);
     if (tn.sort_match)
         launch_sort_passes<true>(keys, vals, max_count, count, sp, L, st);
@@ -486,7 +506,8 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
     uint64_t *f = flags;
     for (uint32_t p = 0; p < split.n; ++p) {
         sort_pass_kernel<true, true, false><<<ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
-                                                                            count, max_count, p, split.shift[p],
+                                                                            count, max_count, p * hist_stride(split.n),
+                                                                            split.shift[p],
                                                                             split.bits[p], ctrl, f,
                                                                             hist_scanned ? 1u : 0u);
         f += (size_t)ntiles << split.bits[p];

@@ -435,7 +435,7 @@ class Batch:
         return t.as_dict()
 
     def set_tuning(self, **knobs):
-        """Change launch choices (suffix_min, eps, views_per_launch, streams, sort_match,
+        """Change launch choices (suffix_min, eps, views_per_launch, streams, sort_match, sort_digit_bits,
         hist_blocks); frames stay the same."""
         t = records.Tuning()
         check(lib().gs_batch_get_tuning(self._h, ctypes.byref(t)))

@@ -186,6 +186,7 @@ class Tuning(ctypes.Structure):
         ("sort_match", ctypes.c_uint32),
         ("hist_blocks", ctypes.c_uint32),
         ("raster_grid", ctypes.c_uint32),
+        ("sort_digit_bits", ctypes.c_uint32),
     ]
 
     def as_dict(self):
