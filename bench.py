@@ -397,6 +397,22 @@ def measure_batched_config(args, mv, keys, stream):
     batch.synchronize(stream=sh)
     batched_ms = e0.elapsed_time(e1) / reps
     batched = [v[2].download() for v in views]
+    # both schedules of the rasteriser, whichever the autotuner kept: per view after its own
+    # binning, or one segmented tile sort over all views and one rasteriser grid
+    by_grid = {}
+    for grid in (0, 1):
+        batch.set_tuning(raster_grid=grid)
+        batch.render(views, stream=sh)
+        batch.synchronize(stream=sh)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            batch.render(views, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        batch.synchronize(stream=sh)
+        by_grid["one_grid_segmented_sort" if grid else "per_view_raster"] = V / (e0.elapsed_time(e1) / reps / 1000.0)
+    batch.set_tuning(**tuning)
     # the plain path: each view alone, one after another on the same stream
     plain_t = {wh: gs300.RenderTarget(*wh) for wh in set(shapes)}
 
@@ -430,6 +446,7 @@ def measure_batched_config(args, mv, keys, stream):
         "batched_mpix_per_s": pixels / (batched_ms / 1000.0) / 1e6,
         "plain_views_per_s": V / (plain_ms / 1000.0), "plain_ms_per_batch": plain_ms,
         "speedup_vs_plain": plain_ms / batched_ms, "frames_identical": same, "tuning": tuning,
+        "views_per_s_by_raster_schedule": by_grid,
     }
 
 

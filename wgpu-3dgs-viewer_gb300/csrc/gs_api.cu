@@ -1102,6 +1102,7 @@ struct gs_batch {
     DevBuf views_dev;                       // PreView per view (device), rebuilt with the graph
     DevBuf group_dev;                       // one control block per multi-view launch
     DevBuf jobs_dev, tile_base_dev;         // per view RasterJob and the prefix of tile counts
+    DevBuf sort_segs_dev, sort_base_dev;    // per view tile-sort segment and the prefix of its blocks
     uint32_t chunks = 0;
     gs::Tuning tuning = gs::default_tuning();
     cudaStream_t capture = nullptr;
@@ -1249,6 +1250,27 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
         GS_CUDA(cudaMemcpy(b->jobs_dev.ptr, jobs.data(), (size_t)n * sizeof(RasterJob), cudaMemcpyHostToDevice));
         GS_CUDA(b->tile_base_dev.ensure((size_t)(n + 1) * 4));
         GS_CUDA(cudaMemcpy(b->tile_base_dev.ptr, tile_base.data(), (size_t)(n + 1) * 4, cudaMemcpyHostToDevice));
+        // With one rasteriser grid, the views' tile sorts run as one segmented sort (one launch per
+        // pass over all views' pairs: keys (view, tile) with depth order kept inside each tile)
+        // when every target fits two tile-sort passes; else each view sorts its own pairs.
+        bool segmented = b->tuning.raster_grid != 0;
+        for (uint32_t i = 0; i < n && segmented; ++i) segmented = tile_sort_segmentable(views[i].width, views[i].height);
+        std::vector<SortSegment> sort_segs(segmented ? n : 0);
+        std::vector<uint32_t> sort_base(n + 1, 0u);
+        if (segmented) {
+            for (uint32_t i = 0; i < n; ++i) {
+                ViewSlot &v = b->slots[i];
+                uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+                const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, ms[i]->n};
+                sort_segs[i] = tile_sort_segment(&seg, 1, views[i].width, views[i].height, v.max_pairs, v.raster_scratch.ptr);
+                sort_base[i + 1] = sort_base[i] + sort_pairs_blocks(v.max_pairs);
+            }
+            GS_CUDA(b->sort_segs_dev.ensure((size_t)n * sizeof(SortSegment)));
+            GS_CUDA(cudaMemcpy(b->sort_segs_dev.ptr, sort_segs.data(), (size_t)n * sizeof(SortSegment),
+                               cudaMemcpyHostToDevice));
+            GS_CUDA(b->sort_base_dev.ensure((size_t)(n + 1) * 4));
+            GS_CUDA(cudaMemcpy(b->sort_base_dev.ptr, sort_base.data(), (size_t)(n + 1) * 4, cudaMemcpyHostToDevice));
+        }
         GS_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
         t_capturing = true;
         t_captured_launches = 0;
@@ -1277,7 +1299,10 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
                                             ms[i]->n};
                     // The graph is replayed for later cameras: binning and raster take only the
                     // display mode and std dev, which are part of the shape key (frame.gt).
-                    if (b->tuning.raster_grid)
+                    if (segmented)
+                        err = launch_binning_front(&seg, 1, raster_mode(uh[i]), views[i].width, views[i].height,
+                                                   v.max_pairs, v.raster_scratch.ptr, vs);
+                    else if (b->tuning.raster_grid)
                         err = launch_binning(&seg, 1, raster_mode(uh[i]), views[i].width, views[i].height, v.max_pairs,
                                              v.raster_scratch.ptr, vs);
                     else
@@ -1290,6 +1315,18 @@ gs_status batch_render_locked(gs_batch *b, const gs_batch_view *views, uint32_t 
         for (uint32_t s = 0; s < nstreams && err == cudaSuccess; ++s) {
             err = cudaEventRecord(b->events[s], b->streams[s]);
             if (err == cudaSuccess) err = cudaStreamWaitEvent(b->capture, b->events[s], 0);
+        }
+        if (err == cudaSuccess && segmented) {
+            err = launch_sort_segments(reinterpret_cast<const SortSegment *>(b->sort_segs_dev.ptr),
+                                       reinterpret_cast<const uint32_t *>(b->sort_base_dev.ptr), n, sort_base[n],
+                                       b->capture);
+            for (uint32_t i = 0; i < n && err == cudaSuccess; ++i) {
+                ViewSlot &v = b->slots[i];
+                uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+                const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, ms[i]->n};
+                err = launch_binning_ranges(&seg, 1, views[i].width, views[i].height, v.max_pairs, v.raster_scratch.ptr,
+                                            b->capture);
+            }
         }
         if (err == cudaSuccess && b->tuning.raster_grid)
             err = launch_raster_views(reinterpret_cast<const RasterJob *>(b->jobs_dev.ptr),

@@ -118,6 +118,27 @@ __host__ __device__ inline uint32_t hist_stride(uint32_t npasses) { return npass
 // control block `owner` is; `alt` holds max_count pairs.
 size_t sort_pairs_flag_words(uint32_t max_count, uint32_t key_bits);
 cudaError_t sort_pairs_begin(Ctrl *ctrl, Ctrl *owner, cudaStream_t st);
+// The split of a tile-pair sort (producers of its digit histograms must use the same one).
+PassSplit tile_split(uint32_t key_bits);
+
+// A segmented sort: many independent two-pass tile-pair sorts (one per view of a batch) in one
+// launch per pass.  A segment is what launch_sort_pairs would sort for one view.
+struct SortSegment {
+    uint2 *data, *alt;          // the view's pairs (sorted in place) and its ping-pong buffer
+    const uint32_t *count;      // device pair count
+    uint32_t max_count;
+    uint32_t shift[2], bits[2]; // tile_split of the view's tile-id bits
+    uint32_t hist_scanned;      // digit histograms already exclusive offsets
+    Ctrl *ctrl;                 // the view's tile-sort control block
+    Ctrl *owner;                // the view's raster control block (its status takes the sort's)
+    uint64_t *flags[2];         // look-back flags of each pass
+};
+// CTAs of one segment (blocks of its pairs at capacity).
+uint32_t sort_pairs_blocks(uint32_t max_count);
+// Both passes over every segment (segs_dev / block_base_dev: device arrays; block_base holds the
+// prefix of the segments' block counts, nseg + 1 entries), then the statuses merged.
+cudaError_t launch_sort_segments(const SortSegment *segs_dev, const uint32_t *block_base_dev, uint32_t nseg,
+                                 uint32_t total_blocks, cudaStream_t st);
 cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits, Ctrl *ctrl,
                               uint64_t *flags, uint2 *alt, cudaStream_t st, bool hist_scanned);
 
@@ -159,6 +180,19 @@ struct RasterJob {
 };
 RasterJob raster_job(const RasterSegment *segs, uint32_t nseg, uint8_t *target, uint32_t width, uint32_t height,
                      uint32_t pitch, uint32_t max_pairs, void *scratch);
+// Binning of one view up to its tile sort (tile rectangles, count scan, pair emission, per-tile
+// counts and ranges or the sort's digit histograms).
+cudaError_t launch_binning_front(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t width,
+                                 uint32_t height, uint32_t max_pairs, void *scratch, cudaStream_t st);
+// The view's tile sort as a segment of a segmented sort (pointer arithmetic on its scratch), and
+// whether its target is small enough for one (two tile-sort passes: at most 65536 tiles).
+SortSegment tile_sort_segment(const RasterSegment *segs, uint32_t nseg, uint32_t width, uint32_t height,
+                              uint32_t max_pairs, void *scratch);
+bool tile_sort_segmentable(uint32_t width, uint32_t height);
+// After the view's tile sort: tile ranges from the sorted pairs where the target has more tiles
+// than the counting path covers (nothing otherwise).
+cudaError_t launch_binning_ranges(const RasterSegment *segs, uint32_t nseg, uint32_t width, uint32_t height,
+                                  uint32_t max_pairs, void *scratch, cudaStream_t st);
 // Binning, tile sort and tile ranges of one view (everything launch_raster does before the
 // rasteriser itself).
 cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t width,

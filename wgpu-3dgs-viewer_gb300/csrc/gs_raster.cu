@@ -1024,7 +1024,7 @@ cudaError_t launch_raster_views(const RasterJob *jobs_dev, const uint32_t *tile_
     return cudaGetLastError();
 }
 
-cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t W,
+cudaError_t launch_binning_front(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t W,
                            uint32_t H, uint32_t max_pairs, void *scratch, cudaStream_t st) {
     uint32_t max_splats = 0;
     for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
@@ -1044,7 +1044,7 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const Raste
         e = cudaMemsetAsync(L.counts, 0, (size_t)L.ntiles * 4, st);
         if (e != cudaSuccess) return e;
     }
-    const PassSplit split = even_split(L.key_bits);
+    const PassSplit split = tile_split(L.key_bits);
     // The emit kernel loops over its ranks grid-stride with equal shares per CTA: one resident
     // wave (at most kEmitBlocks, the per-CTA count area) keeps a second, late wave from
     // doubling the kernel's span.
@@ -1103,15 +1103,45 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const Raste
         count_launches(1);
     }
     prof_mark(kProfBin, false, st);
-    prof_mark(kProfTileSort, true, st);
-    // counting path: tile_scan wrote the digit offsets already scanned; else the emit's counts
-    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_ctrl, L.sort_flags, L.sort_alt, st,
-                          L.counts != nullptr);
-    prof_mark(kProfTileSort, false, st);
-    if (e != cudaSuccess) return e;
-    merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, sort_ctrl);
-    count_launches(1);
-    if (!L.counts) {  // more tiles than the counting path covers: ranges from the sorted pairs
+    return cudaGetLastError();
+}
+
+SortSegment tile_sort_segment(const RasterSegment *segs, uint32_t nseg, uint32_t W, uint32_t H, uint32_t max_pairs,
+                              void *scratch) {
+    uint32_t max_splats = 0;
+    for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
+    const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
+    const PassSplit split = tile_split(L.key_bits);
+    const uint32_t blocks = sort_pairs_blocks(max_pairs);
+    SortSegment S;
+    S.data = L.pairs;
+    S.alt = L.sort_alt;
+    S.count = &L.ctrl->count;
+    S.max_count = max_pairs;
+    for (int p = 0; p < 2; ++p) {
+        S.shift[p] = split.shift[p];
+        S.bits[p] = split.bits[p];
+    }
+    S.hist_scanned = L.counts ? 1u : 0u;
+    S.ctrl = L.sort_ctrl;
+    S.owner = L.ctrl;
+    S.flags[0] = L.sort_flags;
+    S.flags[1] = L.sort_flags + ((size_t)blocks << split.bits[0]);
+    return S;
+}
+
+bool tile_sort_segmentable(uint32_t W, uint32_t H) {
+    const uint32_t tiles = ((W + GS_TILE - 1) / GS_TILE) * ((H + GS_TILE - 1) / GS_TILE);
+    return tile_split(bits_for(tiles > 0 ? tiles - 1 : 0)).n == 2;
+}
+
+cudaError_t launch_binning_ranges(const RasterSegment *segs, uint32_t nseg, uint32_t W, uint32_t H, uint32_t max_pairs,
+                                  void *scratch, cudaStream_t st) {
+    uint32_t max_splats = 0;
+    for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
+    const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
+    cudaError_t e = cudaSuccess;
+    if (L.ntiles > 0 && !L.counts) {  // more tiles than the counting path covers: ranges from the sorted pairs
         prof_mark(kProfRanges, true, st);
         e = cudaMemsetAsync(L.ranges, 0, (size_t)L.ntiles * sizeof(uint2), st);
         if (e != cudaSuccess) return e;
@@ -1123,6 +1153,25 @@ cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const Raste
         count_launches(1);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_binning(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint32_t W, uint32_t H,
+                           uint32_t max_pairs, void *scratch, cudaStream_t st) {
+    uint32_t max_splats = 0;
+    for (uint32_t s = 0; s < nseg; ++s) max_splats += segs[s].max_count;
+    const RasterLayout L = raster_layout(scratch, max_splats, W, H, max_pairs);
+    if (L.ntiles == 0) return cudaSuccess;
+    cudaError_t e = launch_binning_front(segs, nseg, u, W, H, max_pairs, scratch, st);
+    if (e != cudaSuccess) return e;
+    prof_mark(kProfTileSort, true, st);
+    // counting path: tile_scan wrote the digit offsets already scanned; else the emit's counts
+    e = launch_sort_pairs(L.pairs, max_pairs, &L.ctrl->count, L.key_bits, L.sort_ctrl, L.sort_flags, L.sort_alt, st,
+                          L.counts != nullptr);
+    prof_mark(kProfTileSort, false, st);
+    if (e != cudaSuccess) return e;
+    merge_status_kernel<<<1, 1, 0, st>>>(L.ctrl, L.sort_ctrl);
+    count_launches(1);
+    return launch_binning_ranges(segs, nseg, W, H, max_pairs, scratch, st);
 }
 
 cudaError_t launch_raster(const RasterSegment *segs, uint32_t nseg, const RasterMode &u, uint8_t *target,

@@ -178,12 +178,14 @@ __device__ __forceinline__ uint32_t look_back_digit(const uint64_t *flags, uint3
 // MATCH: peers from one match.any instead of a ballot per digit bit.  Measured on GB300, match.any
 // is the cheaper of the two for depth keys (digits spread over many values) and the dearer for
 // tile keys (few distinct digits per warp, and 5 live bits in the last pass).
+// The pass of one block (`block`: the look-back tile; lower blocks are lower, earlier-dispatched
+// CTAs of the same launch).
 template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
-__global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
+__device__ __forceinline__ void sort_pass_block(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
     uint32_t max_count, uint32_t hoff, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
-    uint32_t hist_scanned) {
+    uint32_t hist_scanned, uint32_t block) {
     __shared__ uint2 s_kv[kTileKeys];
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_start[256];
@@ -196,7 +198,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
         s_epoch = *(volatile uint32_t *)&ctrl->epoch;
         s_limit = ctrl->spin_limit;
         s_stall = ctrl->stall_tile;
-        s_tile = blockIdx.x;  // look-back predecessors are lower, earlier-dispatched CTAs
+        s_tile = block;
     }
     for (uint32_t k = tid; k < kSortWarps * 256; k += kSortThreads) (&s_whist[0][0])[k] = 0u;
     __syncthreads();
@@ -321,6 +323,43 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
     }
 }
 
+template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
+__global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
+    const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
+    uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
+    uint32_t max_count, uint32_t hoff, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
+    uint32_t hist_scanned) {
+    // look-back predecessors are lower, earlier-dispatched CTAs
+    sort_pass_block<IN_PACKED, OUT_PACKED, MATCH>(kin, vin, pin, kout, vout, pout, count, max_count, hoff, shift,
+                                                  digit_bits, ctrl, flags, hist_scanned, blockIdx.x);
+}
+
+// One pass of many independent packed pair sorts in a single launch (a segmented sort): segment v
+// owns the CTAs [block_base[v], block_base[v + 1]) and each of them runs the pass on a block of
+// that segment's pairs with the segment's own control block, digit offsets and look-back flags.
+// Pass 0 reads `data` and writes `alt`, pass 1 the reverse, so two passes leave the pairs in place.
+__global__ void __launch_bounds__(kSortThreads, 4) sort_segments_kernel(const SortSegment *__restrict__ segs,
+                                                                        const uint32_t *__restrict__ block_base,
+                                                                        uint32_t nseg, uint32_t pass) {
+    uint32_t lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (block_base[mid] <= blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const SortSegment &S = segs[lo];
+    const uint2 *in = pass ? S.alt : S.data;
+    uint2 *out = pass ? S.data : S.alt;
+    sort_pass_block<true, true, false>(nullptr, nullptr, in, nullptr, nullptr, out, S.count, S.max_count,
+                                       pass * hist_stride(2), S.shift[pass], S.bits[pass], S.ctrl, S.flags[pass],
+                                       S.hist_scanned, blockIdx.x - block_base[lo]);
+}
+
+// Each segment's sort status into the control block of the area it belongs to.
+__global__ void merge_segments_status_kernel(const SortSegment *segs, uint32_t nseg) {
+    for (uint32_t v = threadIdx.x; v < nseg; v += blockDim.x) atomicOr(&segs[v].owner->status, segs[v].ctrl->status);
+}
+
 __global__ void unpack_pairs_kernel(const uint2 *src, uint32_t *kd, uint32_t *vd, const uint32_t *count,
                                     uint32_t max_count) {
     const uint32_t n = load_count(count, max_count);
@@ -349,6 +388,19 @@ PassSplit even_split(uint32_t key_bits) {
         sp.bits[p] = base + (p < extra ? 1u : 0u);
         at += sp.bits[p];
     }
+    return sp;
+}
+
+// Passes of a tile-pair sort: two passes up to 16 key bits (a target of up to 65536 tiles), so the
+// pairs of every such view end where they started and views can share one segmented launch.
+PassSplit tile_split(uint32_t key_bits) {
+    if (key_bits > 16) return even_split(key_bits);
+    PassSplit sp{};
+    sp.n = 2;
+    sp.bits[0] = (key_bits + 1) / 2;
+    sp.bits[1] = key_bits / 2;
+    sp.shift[0] = 0;
+    sp.shift[1] = sp.bits[0];
     return sp;
 }
 
@@ -488,7 +540,19 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
 }
 
 size_t sort_pairs_flag_words(uint32_t max_count, uint32_t key_bits) {
-    return sort_flag_words(max_count, even_split(key_bits));
+    return sort_flag_words(max_count, tile_split(key_bits));
+}
+
+uint32_t sort_pairs_blocks(uint32_t max_count) { return (uint32_t)sort_tiles(max_count); }
+
+cudaError_t launch_sort_segments(const SortSegment *segs_dev, const uint32_t *block_base_dev, uint32_t nseg,
+                                 uint32_t total_blocks, cudaStream_t st) {
+    if (nseg == 0 || total_blocks == 0) return cudaSuccess;
+    for (uint32_t pass = 0; pass < 2; ++pass)
+        sort_segments_kernel<<<total_blocks, kSortThreads, 0, st>>>(segs_dev, block_base_dev, nseg, pass);
+    merge_segments_status_kernel<<<1, 256, 0, st>>>(segs_dev, nseg);
+    count_launches(3);
+    return cudaGetLastError();
 }
 
 cudaError_t sort_pairs_begin(Ctrl *ctrl, Ctrl *owner, cudaStream_t st) {
@@ -499,7 +563,7 @@ cudaError_t sort_pairs_begin(Ctrl *ctrl, Ctrl *owner, cudaStream_t st) {
 
 cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *count, uint32_t key_bits, Ctrl *ctrl,
                               uint64_t *flags, uint2 *alt, cudaStream_t st, bool hist_scanned) {
-    const PassSplit split = even_split(key_bits);
+    const PassSplit split = tile_split(key_bits);
     if (max_count == 0) return cudaSuccess;
     const uint32_t ntiles = (uint32_t)sort_tiles(max_count);
     uint2 *src = data, *dst = alt;
