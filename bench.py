@@ -28,15 +28,12 @@ sys.path.insert(0, os.path.join(REPO, "wgpu-3dgs-viewer_gb300"))
 import numpy as np  # noqa: E402
 
 METRIC = "frames/s @6M splats 1080p"
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the two dominant kernels,
-# from a single-pass ncu capture of the default workload (6M Gaussians, seed 6, 1920x1080; two
-# launches each, averaged).  The preprocess reads every record once; the rasteriser's staged
-# splats come from L2, so its DRAM traffic is far below its algorithmic bytes.
-NCU_TRAFFIC_DEFAULT = {"raster_kernel": 144.2e6, "preprocess": 1.6577e9}
-# The rasteriser's share of the SM instruction-issue peak (ncu sm__inst_issued, % of peak sustained
-# elapsed, 1M-Gaussian 1080p frame): the limit it actually meets (FP32 FLOPs are a minority of its
-# instructions: shared loads, tests, rounding).
-NCU_ISSUE_RASTER = 0.854
+# Counter figures that only ncu can give (DRAM bytes per launch, the rasteriser's share of the SM
+# instruction-issue peak) are not typed in here: each profile summary under profiles/ carries a
+# line "Figures read by bench.py: workload=<n>x<w>x<h>s<seed> <kernel>.<figure>=<value> ..." that
+# states the capture's workload, and profile_figures() reads those lines, so every number in the
+# JSON line names the summary (with its command) that it came from.
+PROFILE_FIGURES_TAG = "Figures read by bench.py:"
 RECORD_BYTES = 224
 SPLAT_BYTES = 48
 
@@ -143,6 +140,38 @@ class ClockSampler:
             "samples": len(sm),
             "power_w_max": max(power) if power else None,
         }
+
+
+def profile_figures():
+    """{(kernel, figure): [(value, workload, summary file)]} from the tagged lines of
+    profiles/*.md (one ncu capture each; the workload token is n x width x height s seed)."""
+    out = {}
+    pdir = os.path.join(REPO, "profiles")
+    if not os.path.isdir(pdir):
+        return out
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(pdir, name)) as f:
+            for line in f:
+                if not line.startswith(PROFILE_FIGURES_TAG):
+                    continue
+                toks = line[len(PROFILE_FIGURES_TAG):].split()
+                kv = dict(t.split("=", 1) for t in toks if "=" in t)
+                wl = kv.pop("workload", None)
+                for key, val in kv.items():
+                    kernel, _, fig = key.rpartition(".")
+                    out.setdefault((kernel, fig), []).append((float(val), wl, "profiles/" + name))
+    return out
+
+
+def profile_figure(figs, kernel, fig, workload=None):
+    """The figure measured at `workload` (any workload when None): (value, workload, source) or
+    None."""
+    for val, wl, src in figs.get((kernel, fig), []):
+        if workload is None or wl == workload:
+            return val, wl, src
+    return None
 
 
 def measured_peaks():
@@ -850,9 +879,14 @@ def main():
         stages["raster"]["tflops"] = flops / (stages["raster"]["ms"] / 1000.0) / 1e12
         stages["raster"]["frac_fp32"] = stages["raster"]["tflops"] / fp32_peak
         stages["raster"]["work_per_frame"] = {k: v / prof["raster"][1] for k, v in counts.items()}
-    default_workload = (args.n, W, H, args.seed) == (6_000_000, 1920, 1080, 6)
-    if default_workload and "preprocess" in stages:
-        stages["preprocess"]["traffic"] = NCU_TRAFFIC_DEFAULT["preprocess"]
+    figs = profile_figures()
+    this_workload = f"{args.n}x{W}x{H}s{args.seed}"
+    pre_traffic = profile_figure(figs, "preprocess_kernel", "dram_bytes", this_workload)
+    if pre_traffic and "preprocess" in stages:
+        stages["preprocess"]["traffic"] = pre_traffic[0]
+        stages["preprocess"]["traffic_source"] = pre_traffic[2]
+    ras_traffic = profile_figure(figs, "raster_kernel", "dram_bytes", this_workload)
+    ras_issue = profile_figure(figs, "raster_kernel", "issue_frac")
     dominant = max(stages, key=lambda s: stages[s]["ms"])
     dom = stages[dominant]
     if dominant == "raster" and "tflops" in dom:
@@ -865,12 +899,14 @@ def main():
             "frac": dom["tflops"] / fp32_peak,
             "peak_kind": f"derived: {sms} SMs x 128 FP32 lanes x 2 x sm_max_mhz {sm_max_mhz:.0f} "
             f"({peak_kind}); no measured FP32 peak exists, the HBM fraction is in stages",
-            "traffic": NCU_TRAFFIC_DEFAULT["raster_kernel"] if default_workload else None,
-            "traffic_note": "DRAM bytes per launch (ncu), against algorithmic bytes "
-            f"{dom['algo_bytes']:.3g}: staged splats are served from L2",
-            "issue_frac": NCU_ISSUE_RASTER,
-            "issue_note": "instructions issued / SM issue peak (ncu sm__inst_issued, 1M case): the kernel is "
-            "issue-bound, so this, not the FP32 FLOP fraction, is its distance to the hardware limit",
+            "traffic": ras_traffic[0] if ras_traffic else None,
+            "traffic_source": ras_traffic[2] if ras_traffic else "no capture of this workload under profiles/",
+            "traffic_note": "DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum), against "
+            f"algorithmic bytes {dom['algo_bytes']:.3g}: staged splats are served from L2",
+            "issue_frac": ras_issue[0] if ras_issue else None,
+            "issue_source": f"{ras_issue[2]} (workload {ras_issue[1]})" if ras_issue else None,
+            "issue_note": "instructions issued / SM issue peak (ncu sm__inst_issued.avg.pct_of_peak_sustained_active): "
+            "the kernel is issue-bound, so this, not the FP32 FLOP fraction, is its distance to the hardware limit",
         }
     else:
         roofline = {
