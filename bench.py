@@ -82,7 +82,9 @@ def workload(args):
         "resolution": [args.width, args.height],
         "record_bytes": RECORD_BYTES,
         "display_mode": "splat",
-        "l2": "inputs larger than L2 (records 1.34 GB >> 129 MB)",
+        "l2": (f"inputs larger than L2 (records {args.n * RECORD_BYTES / 1e9:.2f} GB >> 129 MB)"
+               if args.n * RECORD_BYTES > 129e6 else
+               f"records {args.n * RECORD_BYTES / 1e6:.0f} MB fit the 129 MB L2: no flush between frames"),
     }
 
 

@@ -343,13 +343,13 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
 }
 
 // K3c: every splat writes its (tile, value) pairs at its scanned offset, its kept tiles in
-// row-major order.  A thread walks its own tile rectangle; a splat with more than kWarpEmit
-// tiles is written by its whole warp, 32 pairs at a time, so one large splat does not hold up
-// the others.  Also accumulates the tile-key digit histograms of the tile sort: each CTA loops
-// over chunks of 256 ranks (grid-stride) and adds its shared histograms to the global ones once,
-// which keeps the global atomics on those few hundred bins to a few per CTA.
-constexpr uint32_t kWarpEmit = 32;
-
+// row-major order.  The 32 ranks of a warp own one contiguous run of pairs, and the warp writes
+// that run together: pair r of the run goes to lane r mod 32, which finds its splat by binary
+// search over the warp's exclusive count prefix and its tile from the pair's place in the
+// splat's rectangle.  Stores are consecutive, every lane has a pair in every round but the
+// last, and one large splat is spread over the warp like any other.  Also accumulates the tile
+// counts (or the tile-key digit histograms of the tile sort) in shared memory: each CTA loops
+// over chunks of 256 ranks (grid-stride) and hands its shared bins on once.
 template <bool COUNTS>
 __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
     const uint4 *__restrict__ info, const uint32_t *__restrict__ offsets, const uint32_t *count, uint32_t max_count,
@@ -394,31 +394,42 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
                 cnt = 0;
             }
         }
-        const uint32_t x0 = in.x & 0xFFFFu, y0 = in.x >> 16, w = in.y & 0xFFFFu, h = in.y >> 16;
-        if (cnt > 0 && cnt <= kWarpEmit) {
-            // in.z: tiles kept of a rectangle of at most 16 (bit ty·w + tx); 0 = the whole rectangle
-            uint32_t r = 0;
-            for (uint32_t ty = 0; ty < h; ++ty)
-                for (uint32_t tx = 0; tx < w; ++tx)
-                    if (in.z == 0u || ((in.z >> (ty * w + tx)) & 1u)) {
-                        emit((y0 + ty) * tiles_x + x0 + tx, in.w, o + r);
-                        ++r;
-                    }
+        // warp-exclusive prefix of the counts: this lane's pairs are [excl, excl + cnt) of the run
+        uint32_t incl = cnt;
+#pragma unroll
+        for (uint32_t d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= d) incl += y;
         }
-        // Large rectangles (never masked: masks cover at most 16 tiles), one splat at a time.
-        uint32_t big = __ballot_sync(0xFFFFFFFFu, cnt > kWarpEmit);
-        while (big) {
-            const int src = __ffs(big) - 1;
-            big &= big - 1u;
-            const uint32_t bx0 = __shfl_sync(0xFFFFFFFFu, x0, src), by0 = __shfl_sync(0xFFFFFFFFu, y0, src);
-            const uint32_t bw = __shfl_sync(0xFFFFFFFFu, w, src), bcnt = __shfl_sync(0xFFFFFFFFu, cnt, src);
-            const uint32_t bval = __shfl_sync(0xFFFFFFFFu, in.w, src);
+        const uint32_t excl = incl - cnt, run = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        // a lane's rectangle: x0 | y0 << 16, width, kept-tile mask, value, 1 / width
+        const uint32_t w = in.y & 0xFFFFu;
+        const float inv_w = w ? 1.0f / (float)w : 0.0f;
+        for (uint32_t r0 = 0; r0 < run; r0 += 32) {
+            const uint32_t r = r0 + lane;
+            // the largest lane whose run starts at or before r (a lane with no pairs shares its
+            // start with the next lane, so the search lands on a lane that has pairs)
+            uint32_t src = 0;
+#pragma unroll
+            for (uint32_t step = 16; step >= 1; step >>= 1) {
+                const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, src + step);
+                if (e <= r) src += step;
+            }
+            const uint32_t sx = __shfl_sync(0xFFFFFFFFu, in.x, src), sw = __shfl_sync(0xFFFFFFFFu, w, src);
+            const uint32_t smask = __shfl_sync(0xFFFFFFFFu, in.z, src), sval = __shfl_sync(0xFFFFFFFFu, in.w, src);
+            const float sinv = __shfl_sync(0xFFFFFFFFu, inv_w, src);
+            const uint32_t sex = __shfl_sync(0xFFFFFFFFu, excl, src);
             const uint32_t olo = __shfl_sync(0xFFFFFFFFu, (uint32_t)o, src);
             const uint32_t ohi = __shfl_sync(0xFFFFFFFFu, (uint32_t)(o >> 32), src);
-            const uint64_t bo = ((uint64_t)ohi << 32) | olo;
-            for (uint32_t r = lane; r < bcnt; r += 32) {
-                const uint32_t ty = r / bw, tx = r - ty * bw;
-                emit((by0 + ty) * tiles_x + bx0 + tx, bval, bo + r);
+            if (r < run) {
+                const uint32_t local = r - sex;
+                // in.z: tiles kept of a rectangle of at most 16 (bit ty·w + tx); 0 = all of it
+                const uint32_t pos = smask ? __fns(smask, 0u, (int)local + 1) : local;
+                // row = floor(pos / w), exact in float: pos < 2^24 and the error of 1/w is
+                // far below the 1/w gap between pos/w and the next integer
+                const uint32_t ty = (uint32_t)(((float)pos + 0.5f) * sinv), tx = pos - ty * sw;
+                const uint64_t at = (((uint64_t)ohi << 32) | olo) + local;
+                emit(((sx >> 16) + ty) * tiles_x + (sx & 0xFFFFu) + tx, sval, at);
             }
         }
     }

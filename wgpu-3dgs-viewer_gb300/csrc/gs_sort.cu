@@ -283,7 +283,8 @@ __device__ __forceinline__ void sort_pass_block(
         publish_flag(f, tile, s_stall, pack_flag(epoch, kFlagPrefix, prefix + pub));
     }
     s_start[d] = start;
-    s_gbase[d] = goff + prefix;
+    // key j of the reordered block (j >= start for digit d) goes to goff + prefix + (j - start)
+    s_gbase[d] = goff + prefix - start;
     __syncthreads();
 
     if constexpr (IN_PACKED) {
@@ -311,7 +312,7 @@ __device__ __forceinline__ void sort_pass_block(
     for (uint32_t j = tid; j < valid; j += kSortThreads) {
         const uint2 kv = s_kv[j];
         const uint32_t dd = (kv.x >> shift) & dmask;
-        const uint32_t o = s_gbase[dd] + (j - s_start[dd]);
+        const uint32_t o = s_gbase[dd] + j;
         if (o < n) {  // always true unless a look-back timed out (status already set)
             if constexpr (OUT_PACKED) {
                 pout[o] = kv;
