@@ -29,7 +29,7 @@ def wait_fault(gs):
 
 def test_sort_wait_runs_out_then_recovers(gs, cuda):
     torch = cuda
-    n = 50_000  # 14 sort blocks: tiles 2.. wait on tile 1
+    n = 50_000  # 7 sort blocks of 7680 keys: tiles 2.. wait on tile 1
     rng = np.random.default_rng(1)
     keys = rng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
     vals = np.arange(n, dtype=np.uint32)

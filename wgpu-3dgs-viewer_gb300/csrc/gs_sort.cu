@@ -1,8 +1,9 @@
 // gs_sort.cu — K2: stable LSD onesweep radix sort of u32 keys carrying u32 values.
 //
 // Same contract as the reference RadixSorter (src/radix_sorter.rs:56-96,658-669; kernels
-// src/shader/radix_sort.wgsl:78-529): 8-bit digits, least significant first, 3840 keys per
-// block, stable.  The GB300 design differs: one global-histogram kernel reads the keys once
+// src/shader/radix_sort.wgsl:78-529): 8-bit digits, least significant first, stable; the
+// reference's 3840-key block stays the unit of the depth buffer's padding.  The GB300 design
+// differs: 7680-key pass blocks; one global-histogram kernel reads the keys once
 // for all passes (its last CTA turns the histograms into exclusive digit offsets); each pass is
 // a single kernel that ranks its block warp by warp (match.any, or one ballot per digit bit, so
 // equal digits keep input order), publishes per-digit counts and resolves the block's global
@@ -11,6 +12,7 @@
 // then scatters through shared memory so that each digit's run is written contiguously.
 // The key count may live in device memory (the preprocess instance count), so a whole frame
 // can be enqueued (or graph-captured) without a host round trip.
+#include <atomic>
 #include <mutex>
 
 #include "gs300.h"
@@ -18,11 +20,16 @@
 
 namespace gs {
 
-constexpr uint32_t kSortThreads = 256;
+// A pass block is 512 threads x 15 keys = 7680 keys, two of the reference's 3840-key blocks:
+// longer digit runs in the scatter, and two CTAs (32 warps) per SM.  Threads 0..255 own the
+// digits in the per-digit phases.  The reordered block (60 KB) lives in dynamic shared memory.
+constexpr uint32_t kSortThreads = 512;
 constexpr uint32_t kSortRows = 15;
-constexpr uint32_t kTileKeys = kSortThreads * kSortRows;  // 3840
+constexpr uint32_t kTileKeys = kSortThreads * kSortRows;  // 7680
 constexpr uint32_t kSortWarps = kSortThreads / 32;
-static_assert(kTileKeys == GS_SORT_BLOCK_KVS, "block size must match the reference's");
+constexpr uint32_t kSortCtasPerSm = 2;
+constexpr size_t kSortDynSmem = (size_t)kTileKeys * sizeof(uint2);
+static_assert(kTileKeys % GS_SORT_BLOCK_KVS == 0, "a pass block covers whole blocks of the reference");
 
 __global__ void ctrl_init_kernel(Ctrl *ctrl, int mode, Ctrl *owner, uint32_t arena_words, WaitCfg cfg) {
     ctrl_reset(ctrl, mode, owner ? owner : ctrl, arena_words, cfg);
@@ -32,7 +39,8 @@ __device__ __forceinline__ uint32_t load_count(const uint32_t *count, uint32_t m
     return count ? min(*count, max_count) : max_count;
 }
 
-// Exclusive block scan of one value per thread (256 threads).  `tmp` holds 8 words.
+// Exclusive block scan of one value per thread (WARPS warps).  `tmp` holds WARPS words.
+template <uint32_t WARPS>
 __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, uint32_t *total) {
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     uint32_t x = v;
@@ -44,17 +52,17 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, u
     if (lane == 31) tmp[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        uint32_t t = lane < kSortWarps ? tmp[lane] : 0u;
+        uint32_t t = lane < WARPS ? tmp[lane] : 0u;
 #pragma unroll
-        for (uint32_t o = 1; o < kSortWarps; o <<= 1) {
+        for (uint32_t o = 1; o < WARPS; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, t, o);
             if (lane >= o) t += y;
         }
-        if (lane < kSortWarps) tmp[lane] = t;
+        if (lane < WARPS) tmp[lane] = t;
     }
     __syncthreads();
     const uint32_t before = warp ? tmp[warp - 1] : 0u;
-    *total = tmp[kSortWarps - 1];
+    *total = tmp[WARPS - 1];
     __syncthreads();
     return before + x - v;
 }
@@ -118,7 +126,7 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
     }
     // The last CTA to finish turns the histograms into exclusive digit offsets, once for every
     // block of every pass.
-    __shared__ uint32_t s_last, s_tmp[kSortWarps];
+    __shared__ uint32_t s_last, s_tmp[8];
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&ctrl->ticket[7], 1u) == gridDim.x - 1 ? 1u : 0u;
@@ -128,7 +136,7 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
         for (uint32_t p = 0; p < npasses; ++p) {
             uint32_t total;
             const bool live = threadIdx.x < (1u << sp.bits[p]);
-            const uint32_t off = block_scan_excl(live ? __ldcg(&gh[p * hs + threadIdx.x]) : 0u, s_tmp, &total);
+            const uint32_t off = block_scan_excl<8>(live ? __ldcg(&gh[p * hs + threadIdx.x]) : 0u, s_tmp, &total);
             if (live) gh[p * hs + threadIdx.x] = off;
         }
     }
@@ -186,7 +194,7 @@ __device__ __forceinline__ void sort_pass_block(
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
     uint32_t max_count, uint32_t hoff, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
     uint32_t hist_scanned, uint32_t block) {
-    __shared__ uint2 s_kv[kTileKeys];
+    extern __shared__ uint2 s_kv[];  // kTileKeys pairs (dynamic)
     __shared__ uint32_t s_whist[kSortWarps][256];
     __shared__ uint32_t s_start[256];
     __shared__ uint32_t s_gbase[256];
@@ -250,14 +258,17 @@ __device__ __forceinline__ void sort_pass_block(
     }
     __syncthreads();
 
-    // Thread d owns digit d: per-warp exclusive offsets, block count, publication.
+    // Thread d < 256 owns digit d: per-warp exclusive offsets, block count, publication.
     const uint32_t d = tid;
+    const bool owner = d < 256u;
     uint32_t run = 0;
+    if (owner) {
 #pragma unroll
-    for (uint32_t w = 0; w < kSortWarps; ++w) {
-        const uint32_t c = s_whist[w][d];
-        s_whist[w][d] = run;
-        run += c;
+        for (uint32_t w = 0; w < kSortWarps; ++w) {
+            const uint32_t c = s_whist[w][d];
+            s_whist[w][d] = run;
+            run += c;
+        }
     }
     const uint32_t total = run;
     const uint32_t invalid = (tile == ntiles - 1) ? ntiles * kTileKeys - n : 0u;
@@ -271,20 +282,22 @@ __device__ __forceinline__ void sort_pass_block(
     if (live) publish_flag(f, tile, s_stall, pack_flag(epoch, tile == 0 ? kFlagPrefix : kFlagAggregate, pub));
 
     uint32_t blk_total, hist_total;
-    const uint32_t start = block_scan_excl(total, s_tmp, &blk_total);
+    const uint32_t start = block_scan_excl<kSortWarps>(total, s_tmp, &blk_total);
     // the digit's first place in the output: the histograms hold exclusive offsets already
     // when their producer scanned them (hist_scanned is uniform over the grid)
     // (pass histogram at flat offset hoff; digits above dmask hold no key)
     const uint32_t hv = live ? (&ctrl->hist[0][0])[hoff + d] : 0u;
-    const uint32_t goff = hist_scanned ? hv : block_scan_excl(hv, s_tmp, &hist_total);
+    const uint32_t goff = hist_scanned ? hv : block_scan_excl<kSortWarps>(hv, s_tmp, &hist_total);
     uint32_t prefix = 0;
     if (tile > 0 && live) {
         prefix = look_back_digit(flags + d, tile, epoch, &ctrl->status, fstride, s_limit);
         publish_flag(f, tile, s_stall, pack_flag(epoch, kFlagPrefix, prefix + pub));
     }
-    s_start[d] = start;
-    // key j of the reordered block (j >= start for digit d) goes to goff + prefix + (j - start)
-    s_gbase[d] = goff + prefix - start;
+    if (owner) {
+        s_start[d] = start;
+        // key j of the reordered block (j >= start for digit d) goes to goff + prefix + (j - start)
+        s_gbase[d] = goff + prefix - start;
+    }
     __syncthreads();
 
     if constexpr (IN_PACKED) {
@@ -325,7 +338,7 @@ __device__ __forceinline__ void sort_pass_block(
 }
 
 template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
-__global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
+__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) sort_pass_kernel(
     const uint32_t *__restrict__ kin, const uint32_t *__restrict__ vin, const uint2 *__restrict__ pin,
     uint32_t *__restrict__ kout, uint32_t *__restrict__ vout, uint2 *__restrict__ pout, const uint32_t *count,
     uint32_t max_count, uint32_t hoff, uint32_t shift, uint32_t digit_bits, Ctrl *ctrl, uint64_t *flags,
@@ -339,7 +352,7 @@ __global__ void __launch_bounds__(kSortThreads, 4) sort_pass_kernel(
 // owns the CTAs [block_base[v], block_base[v + 1]) and each of them runs the pass on a block of
 // that segment's pairs with the segment's own control block, digit offsets and look-back flags.
 // Pass 0 reads `data` and writes `alt`, pass 1 the reverse, so two passes leave the pairs in place.
-__global__ void __launch_bounds__(kSortThreads, 4) sort_segments_kernel(const SortSegment *__restrict__ segs,
+__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) sort_segments_kernel(const SortSegment *__restrict__ segs,
                                                                         const uint32_t *__restrict__ block_base,
                                                                         uint32_t nseg, uint32_t pass) {
     uint32_t lo = 0, hi = nseg - 1;
@@ -488,18 +501,18 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
     const uint32_t npasses = sp.n, hs = hist_stride(sp.n);
     uint64_t *f = L.flags;
     if (npasses == 1) {
-        sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+        sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, kSortDynSmem, st>>>(
             keys, vals, nullptr, nullptr, nullptr, L.alt_a, count, max_count, 0, sp.shift[0], sp.bits[0], L.ctrl, f, 1u);
         unpack_pairs_kernel<<<grid_for(max_count), 256, 0, st>>>(L.alt_a, keys, vals, count, max_count);
         count_launches(2);
         return;
     }
     uint2 *src = L.alt_a, *dst = L.alt_b;
-    sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+    sort_pass_kernel<false, true, MATCH><<<L.ntiles, kSortThreads, kSortDynSmem, st>>>(
         keys, vals, nullptr, nullptr, nullptr, src, count, max_count, 0, sp.shift[0], sp.bits[0], L.ctrl, f, 1u);
     f += (size_t)L.ntiles << sp.bits[0];
     for (uint32_t p = 1; p + 1 < npasses; ++p) {
-        sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+        sort_pass_kernel<true, true, MATCH><<<L.ntiles, kSortThreads, kSortDynSmem, st>>>(
             nullptr, nullptr, src, nullptr, nullptr, dst, count, max_count, p * hs, sp.shift[p], sp.bits[p], L.ctrl, f,
             1u);
         f += (size_t)L.ntiles << sp.bits[p];
@@ -507,14 +520,38 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
         src = dst;
         dst = t;
     }
-    sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, 0, st>>>(
+    sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, kSortDynSmem, st>>>(
         nullptr, nullptr, src, keys, vals, nullptr, count, max_count, (npasses - 1) * hs, sp.shift[npasses - 1],
         sp.bits[npasses - 1], L.ctrl, f, 1u);
     count_launches(npasses);
 }
 
+// The pass kernels take kSortDynSmem of dynamic shared memory, above the default 48 KB a launch
+// may ask for: allow it once per device, before the first launch there.
+static cudaError_t ensure_sort_smem() {
+    static std::atomic<uint64_t> ready{0};  // bit d: device d's pass kernels allow kSortDynSmem
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (bit && (ready.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    const void *fns[] = {
+        (const void *)sort_pass_kernel<false, true, false>, (const void *)sort_pass_kernel<true, true, false>,
+        (const void *)sort_pass_kernel<true, false, false>, (const void *)sort_pass_kernel<false, true, true>,
+        (const void *)sort_pass_kernel<true, true, true>,   (const void *)sort_pass_kernel<true, false, true>,
+        (const void *)sort_segments_kernel,
+    };
+    for (const void *f : fns) {
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSortDynSmem);
+        if (e != cudaSuccess) return e;
+    }
+    ready.fetch_or(bit, std::memory_order_acq_rel);
+    return cudaSuccess;
+}
+
 cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                         uint32_t key_bits, void *scratch, cudaStream_t st, int prof_stage, const Tuning *tuning) {
+    if (cudaError_t e = ensure_sort_smem(); e != cudaSuccess) return e;
     const Tuning tn = tuning ? *tuning : default_tuning();
     const uint32_t db = tn.sort_digit_bits < kMinDigitBits   ? kMinDigitBits
                         : tn.sort_digit_bits > kMaxDigitBits ? kMaxDigitBits
@@ -549,8 +586,9 @@ uint32_t sort_pairs_blocks(uint32_t max_count) { return (uint32_t)sort_tiles(max
 cudaError_t launch_sort_segments(const SortSegment *segs_dev, const uint32_t *block_base_dev, uint32_t nseg,
                                  uint32_t total_blocks, cudaStream_t st) {
     if (nseg == 0 || total_blocks == 0) return cudaSuccess;
+    if (cudaError_t e = ensure_sort_smem(); e != cudaSuccess) return e;
     for (uint32_t pass = 0; pass < 2; ++pass)
-        sort_segments_kernel<<<total_blocks, kSortThreads, 0, st>>>(segs_dev, block_base_dev, nseg, pass);
+        sort_segments_kernel<<<total_blocks, kSortThreads, kSortDynSmem, st>>>(segs_dev, block_base_dev, nseg, pass);
     merge_segments_status_kernel<<<1, 256, 0, st>>>(segs_dev, nseg);
     count_launches(3);
     return cudaGetLastError();
@@ -566,11 +604,12 @@ cudaError_t launch_sort_pairs(uint2 *data, uint32_t max_count, const uint32_t *c
                               uint64_t *flags, uint2 *alt, cudaStream_t st, bool hist_scanned) {
     const PassSplit split = tile_split(key_bits);
     if (max_count == 0) return cudaSuccess;
+    if (cudaError_t e = ensure_sort_smem(); e != cudaSuccess) return e;
     const uint32_t ntiles = (uint32_t)sort_tiles(max_count);
     uint2 *src = data, *dst = alt;
     uint64_t *f = flags;
     for (uint32_t p = 0; p < split.n; ++p) {
-        sort_pass_kernel<true, true, false><<<ntiles, kSortThreads, 0, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
+        sort_pass_kernel<true, true, false><<<ntiles, kSortThreads, kSortDynSmem, st>>>(nullptr, nullptr, src, nullptr, nullptr, dst,
                                                                             count, max_count, p * hist_stride(split.n),
                                                                             split.shift[p],
                                                                             split.bits[p], ctrl, f,
