@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=6)
     ap.add_argument("--cpu-baseline-frames", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-single-core", dest="cpu_single_core", action="store_false",
+                    help="skip the 1-thread oracle frame reported beside the all-cores CPU baseline")
     ap.add_argument("--no-tiers", action="store_true")
     ap.add_argument("--batch-views", type=int, default=8)
     ap.add_argument("--serve-inflight", type=int, default=8)
@@ -200,7 +202,7 @@ def cpu_baseline(args, scene, pods, threads):
         u = O.frame_uniforms(pods[k % len(pods)], mt, gt, args.width, args.height)
         O.render(u, scene, R.FORMAT_FP32, args.width, args.height, exp_mode=1, threads=threads)
     dt = time.perf_counter() - t0
-    return {
+    out = {
         "value": frames / dt,
         "unit": "frames/s",
         "cores": threads,
@@ -208,6 +210,15 @@ def cpu_baseline(args, scene, pods, threads):
         "sample": f"{frames} whole frames of the same workload (orbit cameras 0..{frames - 1}), "
         f"oracle/gs_oracle.cpp tile-parallel rasteriser + parallel LSD sort, {dt:.1f} s",
     }
+    if args.cpu_single_core and threads > 1:
+        # the same oracle on one host thread, one whole frame (camera 0)
+        u = O.frame_uniforms(pods[0], mt, gt, args.width, args.height)
+        t0 = time.perf_counter()
+        O.render(u, scene, R.FORMAT_FP32, args.width, args.height, exp_mode=1, threads=1)
+        d1 = time.perf_counter() - t0
+        out["single_core"] = {"value": 1.0 / d1, "unit": "frames/s", "cores": 1,
+                              "sample": f"1 whole frame of the same workload (orbit camera 0), {d1:.1f} s"}
+    return out
 
 
 def measure_tiers(args, scene, pods, stream, plain_fps):
