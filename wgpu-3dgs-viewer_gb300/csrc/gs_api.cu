@@ -1546,7 +1546,7 @@ gs_status gs_batch_autotune(gs_batch *b, const gs_batch_view *views, uint32_t n,
     double best_ms = 0.0;
     gs_status s = measure(best, &best_ms);
     // Candidate values per knob; every combination renders the same frames.
-    const uint32_t suffix_c[] = {1024, 1536, 2048, 3072};
+    const uint32_t suffix_c[] = {768, 1024, 1536, 2048};
     const float eps_c[] = {1e-6f, 1e-5f};
     const uint32_t vpl_c[] = {1, 4, 8, 16};
     const uint32_t streams_c[] = {4, 8, 16};

@@ -72,7 +72,7 @@ cudaError_t launch_ply_convert(const void *vertices, const gs_ply_layout &layout
 // Launch choices that change speed, never results (gs_tuning in the C ABI).  The defaults are
 // the library's; batches can set them or have them picked by gs_batch_autotune.
 struct Tuning {
-    uint32_t suffix_min = 1536;     // raster: tile lists at least this long take the exact early-out
+    uint32_t suffix_min = 1024;     // raster: tile lists at least this long take the exact early-out
     float eps = 1e-6f;              // raster: transmittance that ends the front-to-back walk
     uint32_t views_per_launch = 16; // batch: views per shared-read preprocess launch (1..16)
     uint32_t streams = 16;          // batch: streams the captured graph fans out over (1..16)

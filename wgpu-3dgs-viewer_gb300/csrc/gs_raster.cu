@@ -350,6 +350,22 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
 // last, and one large splat is spread over the warp like any other.  Also accumulates the tile
 // counts (or the tile-key digit histograms of the tile sort) in shared memory: each CTA loops
 // over chunks of 256 ranks (grid-stride) and hands its shared bins on once.
+// Place of the (n+1)-th set bit of a kept-tile mask (at most 16 bits; n < popc(m)): a binary
+// search that halves the window with one popc per step.
+__device__ __forceinline__ uint32_t nth_set_bit16(uint32_t m, uint32_t n) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (uint32_t half = 8; half >= 1; half >>= 1) {
+        const uint32_t c = __popc(m & ((1u << half) - 1u));
+        if (n >= c) {
+            n -= c;
+            m >>= half;
+            pos += half;
+        }
+    }
+    return pos;
+}
+
 template <bool COUNTS>
 __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
     const uint4 *__restrict__ info, const uint32_t *__restrict__ offsets, const uint32_t *count, uint32_t max_count,
@@ -424,7 +440,7 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
             if (r < run) {
                 const uint32_t local = r - sex;
                 // in.z: tiles kept of a rectangle of at most 16 (bit ty·w + tx); 0 = all of it
-                const uint32_t pos = smask ? __fns(smask, 0u, (int)local + 1) : local;
+                const uint32_t pos = smask ? nth_set_bit16(smask, local) : local;
                 // row = floor(pos / w), exact in float: pos < 2^24 and the error of 1/w is
                 // far below the 1/w gap between pos/w and the next integer
                 const uint32_t ty = (uint32_t)(((float)pos + 0.5f) * sinv), tx = pos - ty * sw;
