@@ -68,9 +68,10 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t *tmp, u
 }
 
 // Global digit histograms of all passes in one read of the keys (four keys per thread and
-// iteration, 16-byte loads when the keys are 16-byte aligned).  Per pass, the warp counts the
-// digit of lane 0 with one ballot (the high digits of float depth keys are nearly constant, and
-// same-address shared atomics would serialise) and the other keys with plain shared atomics.
+// iteration, 16-byte loads when the keys are 16-byte aligned).  Low digits are counted with plain
+// shared atomics; for the top digit the warp counts the digit of lane 0 with one ballot (the high
+// digits of float depth keys are nearly constant, and same-address shared atomics would
+// serialise) and the other keys with plain shared atomics.
 __device__ __forceinline__ void hist_add(uint32_t *h, uint32_t k, bool valid, const PassSplit &sp, uint32_t hs,
                                          uint32_t lane) {
     // unrolled over the fixed maximum so every field of the split is read at a constant offset
@@ -78,6 +79,10 @@ __device__ __forceinline__ void hist_add(uint32_t *h, uint32_t k, bool valid, co
     for (uint32_t p = 0; p < kMaxPasses; ++p) {
         if (p >= sp.n) break;
         const uint32_t d = (k >> sp.shift[p]) & ((1u << sp.bits[p]) - 1u);
+        if (p + 1 < sp.n) {  // low digits: spread over the bins, rarely equal within a warp
+            if (valid) atomicAdd(&h[p * hs + d], 1u);
+            continue;
+        }
         const uint32_t d0 = __shfl_sync(0xFFFFFFFFu, d, 0);
         const uint32_t same = __ballot_sync(0xFFFFFFFFu, valid && d == d0);
         if (lane == 0 && same) atomicAdd(&h[p * hs + d0], (uint32_t)__popc(same));
