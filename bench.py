@@ -861,12 +861,14 @@ def main():
     N = args.n
     hbm_peak, sm_max_mhz, peak_kind = measured_peaks()
     algo = {
-        # records read once + key, index and splat record written per visible Gaussian
-        "preprocess": N * RECORD_BYTES + V * (4 + 4 + SPLAT_BYTES),
+        # records read once + key, index, splat record and 16-byte tile record written per visible
+        # Gaussian
+        "preprocess": N * RECORD_BYTES + V * (4 + 4 + SPLAT_BYTES + 16),
         # key histogram read + 4 passes of (key, index) read and written
         "depth_sort": 68.0 * V,
-        # sorted index read, splat gathered and written in draw order, (tile, rank) pairs written
-        "bin": V * (4 + 2 * SPLAT_BYTES) + 8.0 * P,
+        # per rank: sorted index and tile record read, rectangle record and tile count written, the
+        # count scanned in place, rectangle and offset read by the emit; (tile, value) pairs written
+        "bin": V * (4 + 16 + 16 + 4 + 8 + 16 + 4) + 8.0 * P,
         # 2 passes over (tile, value) pairs (digit histograms come from the per-tile counts)
         "tile_sort": 32.0 * P,
         "ranges": 4.0 * P,

@@ -161,6 +161,7 @@ uint32_t default_pairs(uint32_t n, uint32_t w, uint32_t h) {
 struct Model {
     uint32_t n = 0, format = GS_FORMAT_FP32;
     DevBuf records, control, indices, depths, splats, pre_scratch, sort_scratch, selection;
+    DevBuf binfo;  // each visible splat's tiles, written by the preprocess of a one-model view
     int invert = 0;
     bool has_selection = false;
     gs_model_transform_pod model{};
@@ -216,12 +217,20 @@ struct Model {
         return GS_OK;
     }
 
-    // Preprocess + depth sort of this model for one frame.
-    gs_status enqueue(const gs_frame_uniforms &u, cudaStream_t st) {
+    // Preprocess + depth sort of this model for one frame.  `tiles`: the preprocess also stores
+    // each visible splat's tiles for the viewport (binfo), which the binning of a one-model view
+    // gathers instead of the whole splat.
+    gs_status enqueue(const gs_frame_uniforms &u, cudaStream_t st, bool tiles = false) {
+        uint4 *bi = nullptr;
+        if (tiles && n) {
+            GS_CUDA(binfo.ensure((size_t)n * sizeof(uint4)));
+            bi = reinterpret_cast<uint4 *>(binfo.ptr);
+        }
         cudaError_t e = launch_preprocess(u, records.ptr, format, n,
                                           has_selection ? (const uint32_t *)selection.ptr : nullptr, invert,
                                           indirect(), indirect() + 4, (uint32_t *)indices.ptr, (float *)depths.ptr,
-                                          gs_depth_capacity(n), (gs_splat *)splats.ptr, pre_scratch.ptr, st);
+                                          gs_depth_capacity(n), (gs_splat *)splats.ptr, pre_scratch.ptr, st, nullptr,
+                                          bi);
         if (e != cudaSuccess) return cuda_fail(e, "preprocess launch");
         e = launch_sort((uint32_t *)depths.ptr, (uint32_t *)indices.ptr, n, indirect() + 1, kDepthKeyBits,
                         sort_scratch.ptr, st);
@@ -641,10 +650,13 @@ gs_status viewer_render_locked(gs_viewer *v, uint8_t *target, uint32_t w, uint32
     gs_frame_uniforms u;
     s = gs_frame_uniforms_build(&v->frame.camera, &v->model.model, &v->frame.gt, w, h, &u);
     if (s != GS_OK) return s;
-    s = v->model.enqueue(u, st);
+    s = v->model.enqueue(u, st, true);
     if (s != GS_OK) return s;
-    const RasterSegment seg{(const gs_splat *)v->model.splats.ptr, (const uint32_t *)v->model.indices.ptr,
-                            v->model.indirect() + 1, v->model.n};
+    RasterSegment seg{(const gs_splat *)v->model.splats.ptr, (const uint32_t *)v->model.indices.ptr,
+                      v->model.indirect() + 1, v->model.n};
+    seg.binfo = reinterpret_cast<const uint4 *>(v->model.binfo.ptr);
+    seg.binfo_w = w;
+    seg.binfo_h = h;
     const cudaError_t e = launch_raster(&seg, 1, raster_mode(u), target, w, h, pitch, v->frame.max_pairs, v->frame.raster_scratch.ptr,
                                         v->frame.exact_exp, st);
     if (e != cudaSuccess) return cuda_fail(e, "raster launch");

@@ -251,6 +251,99 @@ __device__ __forceinline__ float splat_r2_bound(float alpha, float reach, float 
     return (r2 < std2) ? r2 : std2;
 }
 
+// Tile rectangle of a splat's fragment box; false when it touches no tile.
+__device__ __forceinline__ bool tile_rect(const float4 a, uint32_t tiles_x, uint32_t tiles_y, uint32_t *x0,
+                                          uint32_t *y0, uint32_t *w, uint32_t *h) {
+    const float cx = a.x, cy = a.y, ex = a.z, ey = a.w;
+    if (!(ex >= 0.0f && ey >= 0.0f) || !isfinite(cx) || !isfinite(cy) || !isfinite(ex) || !isfinite(ey))
+        return false;
+    const float inv = 1.0f / (float)GS_TILE;
+    const float fx0 = floorf((cx - ex) * inv), fx1 = floorf((cx + ex) * inv);
+    const float fy0 = floorf((cy - ey) * inv), fy1 = floorf((cy + ey) * inv);
+    const float lx = fmaxf(fx0, 0.0f), hx = fminf(fx1, (float)tiles_x - 1.0f);
+    const float ly = fmaxf(fy0, 0.0f), hy = fminf(fy1, (float)tiles_y - 1.0f);
+    if (lx > hx || ly > hy) return false;
+    *x0 = (uint32_t)lx;
+    *y0 = (uint32_t)ly;
+    *w = (uint32_t)hx - *x0 + 1u;
+    *h = (uint32_t)hy - *y0 + 1u;
+    return true;
+}
+
+// Conservative test whether a splat's fragment ellipse {p : |Q·(p - c)|² <= r2} meets the 16x16
+// tiles of a rectangle.  A tile's box of pixel centres maps to a parallelogram in quad-offset
+// space with the same two edge vectors for every tile; the ellipse becomes the disc of radius
+// sqrt(r2) about the origin, which lies outside the parallelogram when c lies outside the box,
+// so the two meet iff an edge comes within the radius.  The limit carries a small margin, so
+// rounding can only keep a tile, never drop one.
+struct TileCull {
+    float cx, cy, q0, q1, q2, q3, e1x, e1y, e2x, e2y, i1, i2, lim;
+
+    __device__ __forceinline__ TileCull(const float4 a, const float4 q, float r2) {
+        cx = a.x;
+        cy = a.y;
+        q0 = q.x;
+        q1 = q.y;
+        q2 = q.z;
+        q3 = q.w;
+        const float side = (float)(GS_TILE - 1);
+        e1x = q.x * side;
+        e1y = q.z * side;
+        e2x = q.y * side;
+        e2y = q.w * side;
+        i1 = __frcp_rn(e1x * e1x + e1y * e1y);
+        i2 = __frcp_rn(e2x * e2x + e2y * e2y);
+        lim = r2 * 1.002f + 1e-4f;
+    }
+
+    __device__ __forceinline__ bool edge(float ux, float uy, float ex, float ey, float inv) const {
+        float t = -(ux * ex + uy * ey) * inv;
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+        const float px = ux + t * ex, py = uy + t * ey;
+        return px * px + py * py <= lim;
+    }
+
+    // Tile whose first pixel centre is (x0, y0).  Only box edges facing the centre can hold
+    // the point nearest to it, and a linear map keeps which side of an edge a point lies on.
+    __device__ __forceinline__ bool meets(float x0, float y0) const {
+        const float x1 = x0 + (float)(GS_TILE - 1), y1 = y0 + (float)(GS_TILE - 1);
+        const float dx = x0 - cx, dy = y0 - cy;
+        const float ux = q0 * dx + q1 * dy, uy = q2 * dx + q3 * dy;  // corner (x0, y0)
+        if (cx < x0 && edge(ux, uy, e2x, e2y, i2)) return true;                  // left edge
+        if (cx > x1 && edge(ux + e1x, uy + e1y, e2x, e2y, i2)) return true;      // right edge
+        if (cy < y0 && edge(ux, uy, e1x, e1y, i1)) return true;                  // top edge
+        if (cy > y1 && edge(ux + e2x, uy + e2y, e1x, e1y, i1)) return true;      // bottom edge
+        return cx >= x0 && cx <= x1 && cy >= y0 && cy <= y1;                     // centre inside
+    }
+};
+
+// A splat's tiles as the binning stores them: {x0 | y0 << 16, w | h << 16, kept-tile mask,
+// count}.  The footprint is convex and its box meets every tile of the rectangle, so only the
+// corner tiles of a rectangle (up to 16 tiles) can miss it; the mask (bit ty·w + tx) drops those
+// that do, and is 0 when the whole rectangle is kept.
+__device__ __forceinline__ uint4 splat_tile_info(const float4 a, const float4 q, const float4 c, uint32_t tiles_x,
+                                                 uint32_t tiles_y, uint32_t mode, float std2) {
+    uint32_t x0 = 0, y0 = 0, w = 0, h = 0, mask = 0, cnt = 0;
+    if (tile_rect(a, tiles_x, tiles_y, &x0, &y0, &w, &h)) {
+        cnt = w * h;
+        if (mode != GS_DISPLAY_POINT && cnt > 1 && cnt <= 16) {
+            const float r2 =
+                (mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, splat_colour_reach(c.x, c.y, c.z), std2) : std2;
+            const TileCull cull(a, q, r2);
+            mask = cnt == 16 ? 0xFFFFu : (1u << cnt) - 1u;
+#pragma unroll
+            for (uint32_t corner = 0; corner < 4; ++corner) {
+                const uint32_t tx = (corner & 1u) ? w - 1 : 0u, ty = (corner & 2u) ? h - 1 : 0u;
+                if (((corner & 1u) && w == 1) || ((corner & 2u) && h == 1)) continue;  // same tile again
+                if (!cull.meets((float)((x0 + tx) * GS_TILE) + 0.5f, (float)((y0 + ty) * GS_TILE) + 0.5f))
+                    mask &= ~(1u << (ty * w + tx));
+            }
+            cnt = __popc(mask);
+        }
+    }
+    return make_uint4(x0 | (y0 << 16), w | (h << 16), mask, cnt);
+}
+
 // Scratch carving: 256-byte aligned sub-allocations.
 __host__ __device__ __forceinline__ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 

@@ -42,7 +42,7 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
                               uint32_t n, const uint32_t *selection, int invert, uint32_t *indirect,
                               uint32_t *dispatch, uint32_t *indices, float *depths,
                               uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st,
-                              const gs_frame_uniforms *u_dev = nullptr);
+                              const gs_frame_uniforms *u_dev = nullptr, uint4 *binfo = nullptr);
 
 // Several views of one model in one launch (records read once).  A view's scratch is the one
 // launch_preprocess takes for that model; `group` is a zeroed Ctrl-sized block for the launch.
@@ -156,6 +156,10 @@ struct RasterSegment {
     const uint32_t *sorted_index; // draw order
     const uint32_t *count;        // device: number of entries in sorted_index
     uint32_t max_count;           // capacity of sorted_index
+    // Optional: each visible splat's tiles as its preprocess stored them for a binfo_w x
+    // binfo_h target (indexed by Gaussian index); used when the binning's target matches.
+    const uint4 *binfo = nullptr;
+    uint32_t binfo_w = 0, binfo_h = 0;
 };
 size_t raster_scratch_bytes(uint32_t max_splats, uint32_t width, uint32_t height, uint32_t max_pairs);
 // exact_exp: 1 = the portable exp (bit-identical with the CPU oracle), 0 = the SFU exp.

@@ -35,6 +35,8 @@ struct PreParams {
     float *depths;
     uint32_t depth_cap;
     gs_splat *splats;
+    uint4 *binfo;  // optional: each visible splat's tiles (splat_tile_info) for the viewport's tiles
+    uint32_t tiles_x, tiles_y;
     Ctrl *ctrl;
     uint64_t *flags;
 };
@@ -352,8 +354,10 @@ __device__ __forceinline__ bool gaussian_visible(const gs_frame_uniforms &u, con
 }
 
 // Per-instance vertex work (render.wesl:75-130): the splat record of a visible Gaussian.
+// With `binfo`, also the splat's tiles for a tiles_x x tiles_y grid, as the binning works them out.
 template <uint32_t FMT>
-__device__ __forceinline__ void write_splat(const gs_frame_uniforms &u, const Rec &g, Proj &pr, gs_splat *out) {
+__device__ __forceinline__ void write_splat(const gs_frame_uniforms &u, const Rec &g, Proj &pr, gs_splat *out,
+                                            uint4 *binfo = nullptr, uint32_t tiles_x = 0, uint32_t tiles_y = 0) {
     float rgba[4];
     view_color<FMT>(u, g, pr.world, rgba);
     const float W = u.viewport[0], H = u.viewport[1];
@@ -406,10 +410,14 @@ __device__ __forceinline__ void write_splat(const gs_frame_uniforms &u, const Re
             ey = -1.0f;
         }
     }
+    const float4 a = make_float4(cx, cy, ex, ey), q = make_float4(q0, q1, q2, q3);
+    const float4 c =
+        make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f, rgba[3]);
     float4 *sp = reinterpret_cast<float4 *>(out);
-    sp[0] = make_float4(cx, cy, ex, ey);
-    sp[1] = make_float4(q0, q1, q2, q3);
-    sp[2] = make_float4(clamp01(rgba[0]) * 255.0f, clamp01(rgba[1]) * 255.0f, clamp01(rgba[2]) * 255.0f, rgba[3]);
+    sp[0] = a;
+    sp[1] = q;
+    sp[2] = c;
+    if (binfo) *binfo = splat_tile_info(a, q, c, tiles_x, tiles_y, u.display_mode, std2);
 }
 
 // Selection (preprocess.wesl:68-78): a Gaussian takes part when its bit differs from `invert`.
@@ -571,7 +579,7 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     }
 
     // ---- per-instance vertex work (render.wesl:75-130), written at the Gaussian's index ----
-    if (vis && P.splats) write_splat<FMT>(u, g, pr, P.splats + i);
+    if (vis && P.splats) write_splat<FMT>(u, g, pr, P.splats + i, P.binfo ? P.binfo + i : nullptr, P.tiles_x, P.tiles_y);
 
     // ---- global offset: warp 0 looks back over the predecessors' published counts ----
     __syncthreads();
@@ -836,7 +844,7 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
                               uint32_t n, const uint32_t *selection, int invert, uint32_t *indirect,
                               uint32_t *dispatch, uint32_t *indices, float *depths,
                               uint32_t depth_cap, gs_splat *splats, void *scratch, cudaStream_t st,
-                              const gs_frame_uniforms *u_dev) {
+                              const gs_frame_uniforms *u_dev, uint4 *binfo) {
     Ctrl *ctrl = reinterpret_cast<Ctrl *>(scratch);
     uint64_t *flags = reinterpret_cast<uint64_t *>((uint8_t *)scratch + align_up(sizeof(Ctrl), 256));
     ctrl_init_kernel<<<1, 256, 0, st>>>(ctrl, 1, nullptr, kKeepArena, wait_config());
@@ -860,6 +868,10 @@ cudaError_t launch_preprocess(const gs_frame_uniforms &u, const void *records, u
     P.depths = depths;
     P.depth_cap = depth_cap;
     P.splats = splats;
+    // the tile records need the viewport on the host (graph-captured uniforms are not read here)
+    P.binfo = u_dev ? nullptr : binfo;
+    P.tiles_x = ((uint32_t)u.viewport[0] + GS_TILE - 1) / GS_TILE;
+    P.tiles_y = ((uint32_t)u.viewport[1] + GS_TILE - 1) / GS_TILE;
     P.ctrl = ctrl;
     P.flags = flags;
     prof_mark(kProfPreprocess, true, st);

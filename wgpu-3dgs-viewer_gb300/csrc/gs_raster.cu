@@ -134,122 +134,44 @@ Tuning default_tuning() {
     return t;
 }
 
-// Tile rectangle of a splat's fragment box; false when it touches no tile.
-__device__ __forceinline__ bool tile_rect(const float4 a, uint32_t tiles_x, uint32_t tiles_y, uint32_t *x0,
-                                          uint32_t *y0, uint32_t *w, uint32_t *h) {
-    const float cx = a.x, cy = a.y, ex = a.z, ey = a.w;
-    if (!(ex >= 0.0f && ey >= 0.0f) || !isfinite(cx) || !isfinite(cy) || !isfinite(ex) || !isfinite(ey))
-        return false;
-    const float inv = 1.0f / (float)GS_TILE;
-    const float fx0 = floorf((cx - ex) * inv), fx1 = floorf((cx + ex) * inv);
-    const float fy0 = floorf((cy - ey) * inv), fy1 = floorf((cy + ey) * inv);
-    const float lx = fmaxf(fx0, 0.0f), hx = fminf(fx1, (float)tiles_x - 1.0f);
-    const float ly = fmaxf(fy0, 0.0f), hy = fminf(fy1, (float)tiles_y - 1.0f);
-    if (lx > hx || ly > hy) return false;
-    *x0 = (uint32_t)lx;
-    *y0 = (uint32_t)ly;
-    *w = (uint32_t)hx - *x0 + 1u;
-    *h = (uint32_t)hy - *y0 + 1u;
-    return true;
-}
-
-// Conservative test whether a splat's fragment ellipse {p : |Q·(p - c)|² <= r2} meets the 16x16
-// tiles of a rectangle.  A tile's box of pixel centres maps to a parallelogram in quad-offset
-// space with the same two edge vectors for every tile; the ellipse becomes the disc of radius
-// sqrt(r2) about the origin, which lies outside the parallelogram when c lies outside the box,
-// so the two meet iff an edge comes within the radius.  The limit carries a small margin, so
-// rounding can only keep a tile, never drop one.
-struct TileCull {
-    float cx, cy, q0, q1, q2, q3, e1x, e1y, e2x, e2y, i1, i2, lim;
-
-    __device__ __forceinline__ TileCull(const float4 a, const float4 q, float r2) {
-        cx = a.x;
-        cy = a.y;
-        q0 = q.x;
-        q1 = q.y;
-        q2 = q.z;
-        q3 = q.w;
-        const float side = (float)(GS_TILE - 1);
-        e1x = q.x * side;
-        e1y = q.z * side;
-        e2x = q.y * side;
-        e2y = q.w * side;
-        i1 = __frcp_rn(e1x * e1x + e1y * e1y);
-        i2 = __frcp_rn(e2x * e2x + e2y * e2y);
-        lim = r2 * 1.002f + 1e-4f;
-    }
-
-    __device__ __forceinline__ bool edge(float ux, float uy, float ex, float ey, float inv) const {
-        float t = -(ux * ex + uy * ey) * inv;
-        t = fminf(fmaxf(t, 0.0f), 1.0f);
-        const float px = ux + t * ex, py = uy + t * ey;
-        return px * px + py * py <= lim;
-    }
-
-    // Tile whose first pixel centre is (x0, y0).  Only box edges facing the centre can hold
-    // the point nearest to it, and a linear map keeps which side of an edge a point lies on.
-    __device__ __forceinline__ bool meets(float x0, float y0) const {
-        const float x1 = x0 + (float)(GS_TILE - 1), y1 = y0 + (float)(GS_TILE - 1);
-        const float dx = x0 - cx, dy = y0 - cy;
-        const float ux = q0 * dx + q1 * dy, uy = q2 * dx + q3 * dy;  // corner (x0, y0)
-        if (cx < x0 && edge(ux, uy, e2x, e2y, i2)) return true;                  // left edge
-        if (cx > x1 && edge(ux + e1x, uy + e1y, e2x, e2y, i2)) return true;      // right edge
-        if (cy < y0 && edge(ux, uy, e1x, e1y, i1)) return true;                  // top edge
-        if (cy > y1 && edge(ux + e2x, uy + e2y, e1x, e1y, i1)) return true;      // bottom edge
-        return cx >= x0 && cx <= x1 && cy >= y0 && cy <= y1;                     // centre inside
-    }
-};
-
 // K3a: per draw rank, the splat's tile rectangle, the corner tiles its footprint misses, and
-// its tile count.  Several models first copy their splats into draw order.  The first segment's
-// launch (arena non-null) also clears the flag-arena words the call must clear, before the
-// scan and the tile sort read any flag.
+// its tile count.  With `binfo` (one view of one model, its preprocess having stored each
+// visible splat's tiles) the rank gathers that 16-byte record; otherwise it gathers the 48-byte
+// splat and works the tiles out here.  Several models first copy their splats into draw order.
+// The first segment's launch (arena non-null) also clears the flag-arena words the call must
+// clear, before the scan and the tile sort read any flag.
 __global__ void __launch_bounds__(kBinThreads) bin_count_kernel(
-    const gs_splat *__restrict__ splats, const uint32_t *__restrict__ sorted_index, const uint32_t *count,
-    uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, int direct, uint32_t tiles_x,
-    uint32_t tiles_y, uint32_t mode, float std2, uint4 *__restrict__ info, uint32_t *__restrict__ counts,
-    const Ctrl *owner, uint64_t *arena) {
+    const gs_splat *__restrict__ splats, const uint4 *__restrict__ binfo, const uint32_t *__restrict__ sorted_index,
+    const uint32_t *count, uint32_t max_count, uint32_t rank_offset, gs_splat *__restrict__ sorted_out, int direct,
+    uint32_t tiles_x, uint32_t tiles_y, uint32_t mode, float std2, uint4 *__restrict__ info,
+    uint32_t *__restrict__ counts, const Ctrl *owner, uint64_t *arena) {
     if (arena) arena_clear(owner, arena);
     const uint32_t n = count ? min(*count, max_count) : max_count;
     const uint32_t k = blockIdx.x * kBinThreads + threadIdx.x;
     if (k >= n) return;
     // Indices come from the depth sort; the bound check only matters if that sort timed out.
     const uint32_t gi = sorted_index[k];
-    uint32_t cnt = 0, x0 = 0, y0 = 0, w = 0, h = 0, mask = 0;
+    uint4 t = make_uint4(0u, 0u, 0u, 0u);  // x0 | y0 << 16, w | h << 16, mask, count
     if (gi < max_count) {
-        // all three 16-byte parts in one round trip (the colour bounds the corner-tile test)
-        const float4 *src = reinterpret_cast<const float4 *>(splats + gi);
-        const float4 a = __ldg(src);
-        const float4 q = __ldg(src + 1);
-        const float4 c = __ldg(src + 2);
-        if (!direct) {
-            float4 *dst = reinterpret_cast<float4 *>(sorted_out + rank_offset + k);
-            dst[0] = a;
-            dst[1] = q;
-            dst[2] = c;
-        }
-        if (tile_rect(a, tiles_x, tiles_y, &x0, &y0, &w, &h)) {
-            cnt = w * h;
-            // The footprint is convex and its box meets every tile of the rectangle, so only the
-            // corner tiles of a rectangle (up to 16 tiles) can miss it; drop those that do.
-            if (mode != GS_DISPLAY_POINT && cnt > 1 && cnt <= 16) {
-                const float r2 =
-                    (mode == GS_DISPLAY_SPLAT) ? splat_r2_bound(c.w, splat_colour_reach(c.x, c.y, c.z), std2) : std2;
-                const TileCull cull(a, q, r2);
-                mask = cnt == 16 ? 0xFFFFu : (1u << cnt) - 1u;
-#pragma unroll
-                for (uint32_t corner = 0; corner < 4; ++corner) {
-                    const uint32_t tx = (corner & 1u) ? w - 1 : 0u, ty = (corner & 2u) ? h - 1 : 0u;
-                    if (((corner & 1u) && w == 1) || ((corner & 2u) && h == 1)) continue;  // same tile again
-                    if (!cull.meets((float)((x0 + tx) * GS_TILE) + 0.5f, (float)((y0 + ty) * GS_TILE) + 0.5f))
-                        mask &= ~(1u << (ty * w + tx));
-                }
-                cnt = __popc(mask);
+        if (binfo) {
+            t = binfo[gi];
+        } else {
+            // all three 16-byte parts in one round trip (the colour bounds the corner-tile test)
+            const float4 *src = reinterpret_cast<const float4 *>(splats + gi);
+            const float4 a = __ldg(src);
+            const float4 q = __ldg(src + 1);
+            const float4 c = __ldg(src + 2);
+            if (!direct) {
+                float4 *dst = reinterpret_cast<float4 *>(sorted_out + rank_offset + k);
+                dst[0] = a;
+                dst[1] = q;
+                dst[2] = c;
             }
+            t = splat_tile_info(a, q, c, tiles_x, tiles_y, mode, std2);
         }
     }
-    info[k] = make_uint4(x0 | (y0 << 16), w | (h << 16), mask, direct ? gi : rank_offset + k);
-    counts[k] = cnt;
+    info[k] = make_uint4(t.x, t.y, t.z, direct ? gi : rank_offset + k);
+    counts[k] = t.w;
 }
 
 // K3b: exclusive scan of the tile counts in place (decoupled look-back over 4096-count tiles);
@@ -1101,10 +1023,12 @@ cudaError_t launch_binning_front(const RasterSegment *segs, uint32_t nseg, const
             ctrl_init_kernel<<<1, 32, 0, st>>>(L.ctrl, 0, nullptr, kKeepArena, cfg);
             count_launches(1);
         }
-        bin_count_kernel<<<blocks, kBinThreads, 0, st>>>(g.splats, g.sorted_index, g.count, g.max_count, rank_offset,
-                                                         L.sorted, direct, L.tiles_x, L.tiles_y, u.display_mode,
-                                                         u.std_dev * u.std_dev, L.info, L.offsets, L.ctrl,
-                                                         cleared ? nullptr : L.flags);
+        // a stored tile record is only for the target the preprocess was given (one model)
+        const uint4 *binfo = direct && g.binfo && g.binfo_w == W && g.binfo_h == H ? g.binfo : nullptr;
+        bin_count_kernel<<<blocks, kBinThreads, 0, st>>>(g.splats, binfo, g.sorted_index, g.count, g.max_count,
+                                                         rank_offset, L.sorted, direct, L.tiles_x, L.tiles_y,
+                                                         u.display_mode, u.std_dev * u.std_dev, L.info, L.offsets,
+                                                         L.ctrl, cleared ? nullptr : L.flags);
         cleared = true;
         const uint32_t scan_blocks = (g.max_count + kScanTile - 1) / kScanTile;
         bin_scan_kernel<<<scan_blocks, 256, 0, st>>>(L.offsets, g.count, g.max_count, L.ctrl, L.flags);
