@@ -381,7 +381,8 @@ typedef struct gs_tuning {
                                   runs of equal digits per block at the price of more passes */
 } gs_tuning;
 /* The library's defaults (GS300_SUFFIX_MIN / GS300_SUFFIX_EPS override the raster knobs,
- * GS300_SORT_DIGIT_BITS the depth sort's digit width). */
+ * GS300_SORT_DIGIT_BITS the depth sort's digit width, GS300_SORT_MATCH its ranking and
+ * GS300_HIST_BLOCKS its key-histogram grid). */
 gs_status gs_tuning_default(gs_tuning *out);
 /* GS_ERR_INVALID_ARG outside the ranges above.  The next render re-captures the graph. */
 gs_status gs_batch_set_tuning(gs_batch *batch, const gs_tuning *tuning);

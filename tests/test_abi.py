@@ -139,7 +139,7 @@ def test_scratch_sizes_grow_with_problem(gs):
 def test_tuning_default(gs):
     t = gs.tuning_default()
     assert t == {"suffix_min": 1024, "eps": pytest.approx(1e-6), "views_per_launch": 16, "streams": 16,
-                 "sort_match": 1, "hist_blocks": 0, "raster_grid": 0, "sort_digit_bits": 8}
+                 "sort_match": 0, "hist_blocks": 0, "raster_grid": 0, "sort_digit_bits": 8}
 
 
 def test_wait_fault_hook_validates_and_restores(gs):

@@ -76,7 +76,7 @@ struct Tuning {
     float eps = 1e-6f;              // raster: transmittance that ends the front-to-back walk
     uint32_t views_per_launch = 16; // batch: views per shared-read preprocess launch (1..16)
     uint32_t streams = 16;          // batch: streams the captured graph fans out over (1..16)
-    uint32_t sort_match = 1;        // depth sort: 1 = match.any ranking, 0 = a ballot per digit bit
+    uint32_t sort_match = 0;        // depth sort: 1 = match.any ranking, 0 = a ballot per digit bit
     uint32_t sort_digit_bits = 8;   // depth sort: widest digit of a pass (6..8), bits spread evenly
     uint32_t hist_blocks = 0;       // depth sort: key-histogram grid (0 = by key count, <= 1216)
     uint32_t raster_grid = 0;       // batch: 0 = each view rasterised after its own binning,

@@ -131,6 +131,7 @@ Tuning default_tuning() {
     if (const char *v = getenv("GS300_SUFFIX_EPS")) t.eps = strtof(v, nullptr);
     if (const char *v = getenv("GS300_SORT_DIGIT_BITS")) t.sort_digit_bits = (uint32_t)strtoul(v, nullptr, 10);
     if (const char *v = getenv("GS300_HIST_BLOCKS")) t.hist_blocks = (uint32_t)strtoul(v, nullptr, 10);
+    if (const char *v = getenv("GS300_SORT_MATCH")) t.sort_match = (uint32_t)strtoul(v, nullptr, 10) ? 1u : 0u;
     return t;
 }
 
