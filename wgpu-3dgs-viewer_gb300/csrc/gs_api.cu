@@ -1062,6 +1062,7 @@ struct ViewSlot {
     const Model *model = nullptr;
     uint32_t w = 0, h = 0;
     DevBuf control, indices, depths, splats, pre_scratch, sort_scratch, raster_scratch;
+    DevBuf binfo;  // tile records of a view preprocessed alone (serving); grows like the others
     uint32_t max_pairs = 0;
 
     // Buffers of one view of `m` at w x h; *changed is set when any pointer changed (a captured
@@ -1717,16 +1718,22 @@ gs_status server_prepare(gs_server *sv, ServerReq &r, ServerSlot &sl, uint8_t **
     return gs_frame_uniforms_build(&r.camera, &r.model->model, &gt, r.w, r.h, u);
 }
 
-// Depth sort, raster, read-back and completion event of a request whose preprocess is enqueued.
+// Depth sort, raster, read-back and completion event of a request whose preprocess is enqueued
+// (`tiles`: that preprocess also stored the splats' tile records in the slot's binfo).
 gs_status server_finish(gs_server *sv, ServerReq &r, ServerSlot &sl, uint8_t *target, uint32_t pitch,
-                        const gs_frame_uniforms &u) {
+                        const gs_frame_uniforms &u, bool tiles) {
     const Model *m = r.model;
     ViewSlot &v = sl.view;
     uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
     cudaError_t e = launch_sort((uint32_t *)v.depths.ptr, (uint32_t *)v.indices.ptr, m->n, ind + 1, kDepthKeyBits,
                                 v.sort_scratch.ptr, sl.stream);
     if (e == cudaSuccess) {
-        const RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
+        RasterSegment seg{(const gs_splat *)v.splats.ptr, (const uint32_t *)v.indices.ptr, ind + 1, m->n};
+        if (tiles) {
+            seg.binfo = reinterpret_cast<const uint4 *>(v.binfo.ptr);
+            seg.binfo_w = r.w;
+            seg.binfo_h = r.h;
+        }
         e = launch_raster(&seg, 1, raster_mode(u), target, r.w, r.h, pitch, v.max_pairs, v.raster_scratch.ptr,
                           sv->mv->frame.exact_exp, sl.stream);
     }
@@ -1747,13 +1754,14 @@ gs_status server_launch(gs_server *sv, ServerReq &r, ServerSlot &sl) {
     const Model *m = r.model;
     ViewSlot &v = sl.view;
     uint32_t *ind = reinterpret_cast<uint32_t *>(v.control.ptr);
+    GS_CUDA(v.binfo.ensure((size_t)(m->n ? m->n : 1) * sizeof(uint4)));
     const cudaError_t e = launch_preprocess(u, m->records.ptr, m->format, m->n,
                                             m->has_selection ? (const uint32_t *)m->selection.ptr : nullptr, m->invert,
                                             ind, ind + 4, (uint32_t *)v.indices.ptr, (float *)v.depths.ptr,
                                             gs_depth_capacity(m->n), (gs_splat *)v.splats.ptr, v.pre_scratch.ptr,
-                                            sl.stream);
+                                            sl.stream, nullptr, reinterpret_cast<uint4 *>(v.binfo.ptr));
     if (e != cudaSuccess) return cuda_fail(e, "server launch");
-    return server_finish(sv, r, sl, target, pitch, u);
+    return server_finish(sv, r, sl, target, pitch, u, true);
 }
 
 // Dynamic batching: admitted requests of one scene (group[0] leads) share one preprocess launch
@@ -1802,7 +1810,7 @@ gs_status server_launch_group(gs_server *sv, const std::vector<std::pair<ServerR
     for (size_t k = 0; k < nv; ++k) {
         ServerSlot &sl = *group[k].second;
         if (k > 0) GS_CUDA(cudaStreamWaitEvent(sl.stream, lead.pre_done, 0));
-        const gs_status s = server_finish(sv, *group[k].first, sl, targets[k], pitches[k], us[k]);
+        const gs_status s = server_finish(sv, *group[k].first, sl, targets[k], pitches[k], us[k], false);
         if (s != GS_OK) return s;
     }
     return GS_OK;

@@ -501,7 +501,9 @@ static uint32_t grid_for(uint32_t max_count) {
     return blocks ? blocks : 1;
 }
 
-template <bool MATCH>
+// MATCH_LAST: the last pass ranks by match.any whatever MATCH says (the top digit of float depth
+// keys takes a few values per warp, where one match.any is cheaper than a ballot per bit).
+template <bool MATCH, bool MATCH_LAST>
 static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_count, const uint32_t *count,
                                const PassSplit &sp, const SortLayout &L, cudaStream_t st) {
     const uint32_t npasses = sp.n, hs = hist_stride(sp.n);
@@ -526,7 +528,7 @@ static void launch_sort_passes(uint32_t *keys, uint32_t *vals, uint32_t max_coun
         src = dst;
         dst = t;
     }
-    sort_pass_kernel<true, false, MATCH><<<L.ntiles, kSortThreads, kSortDynSmem, st>>>(
+    sort_pass_kernel<true, false, MATCH || MATCH_LAST><<<L.ntiles, kSortThreads, kSortDynSmem, st>>>(
         nullptr, nullptr, src, keys, vals, nullptr, count, max_count, (npasses - 1) * hs, sp.shift[npasses - 1],
         sp.bits[npasses - 1], L.ctrl, f, 1u);
     count_launches(npasses);
@@ -575,10 +577,13 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     if (tn.hist_blocks) hist_blocks = tn.hist_blocks < 152 * 8 ? tn.hist_blocks : 152 * 8;
     sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, sp, L.ctrl, L.flags);
     count_launches(1);
+    // Keys of kDepthKeyBits are the render path's float depth keys (1 - ndc.z).
     if (tn.sort_match)
-        launch_sort_passes<true>(keys, vals, max_count, count, sp, L, st);
+        launch_sort_passes<true, true>(keys, vals, max_count, count, sp, L, st);
+    else if (key_bits == kDepthKeyBits)
+        launch_sort_passes<false, true>(keys, vals, max_count, count, sp, L, st);
     else
-        launch_sort_passes<false>(keys, vals, max_count, count, sp, L, st);
+        launch_sort_passes<false, false>(keys, vals, max_count, count, sp, L, st);
     prof_mark(prof_stage, false, st);
     return cudaGetLastError();
 }
