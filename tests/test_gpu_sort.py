@@ -83,7 +83,7 @@ def test_sort_device_count_leaves_tail_untouched(gs, cuda, count):
     assert np.array_equal(k[count:], keys[count:]) and np.array_equal(v[count:], vals[count:])
 
 
-@pytest.mark.parametrize("bits", [1, 7, 13, 16, 20])
+@pytest.mark.parametrize("bits", [1, 7, 13, 16, 20, 30])  # 30: depth keys, match.any in the last pass
 def test_sort_partial_key_bits(gs, cuda, bits):
     rng = np.random.default_rng(bits)
     n = 70000
