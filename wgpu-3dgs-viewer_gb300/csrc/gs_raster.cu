@@ -265,30 +265,28 @@ __global__ void __launch_bounds__(256) bin_scan_kernel(uint32_t *__restrict__ da
     }
 }
 
+// Place, in its w x h rectangle, of the n-th kept tile of a splat (n < its tile count).  The
+// kept-tile mask (splat_tile_info) only ever drops corner tiles, at places 0, w-1, (h-1)w and
+// hw-1, so the place is n moved past each dropped corner at or before it, in increasing order
+// (the last corner has no place after it): cheaper than a general n-th-set-bit search.
+__device__ __forceinline__ uint32_t kept_tile_place(uint32_t m, uint32_t w, uint32_t h, uint32_t n) {
+    uint32_t pos = n;
+    if (!(m & 1u)) ++pos;
+    if (w > 1u && !((m >> (w - 1u)) & 1u) && pos >= w - 1u) ++pos;
+    const uint32_t c2 = (h - 1u) * w;
+    if (h > 1u && !((m >> c2) & 1u) && pos >= c2) ++pos;
+    return pos;
+}
+
 // K3c: every splat writes its (tile, value) pairs at its scanned offset, its kept tiles in
 // row-major order.  The 32 ranks of a warp own one contiguous run of pairs, and the warp writes
 // that run together: pair r of the run goes to lane r mod 32, which finds its splat by binary
 // search over the warp's exclusive count prefix and its tile from the pair's place in the
-// splat's rectangle.  Stores are consecutive, every lane has a pair in every round but the
-// last, and one large splat is spread over the warp like any other.  Also accumulates the tile
-// counts (or the tile-key digit histograms of the tile sort) in shared memory: each CTA loops
-// over chunks of 256 ranks (grid-stride) and hands its shared bins on once.
-// Place of the (n+1)-th set bit of a kept-tile mask (at most 16 bits; n < popc(m)): a binary
-// search that halves the window with one popc per step.
-__device__ __forceinline__ uint32_t nth_set_bit16(uint32_t m, uint32_t n) {
-    uint32_t pos = 0;
-#pragma unroll
-    for (uint32_t half = 8; half >= 1; half >>= 1) {
-        const uint32_t c = __popc(m & ((1u << half) - 1u));
-        if (n >= c) {
-            n -= c;
-            m >>= half;
-            pos += half;
-        }
-    }
-    return pos;
-}
-
+// splat's rectangle (its kept tiles skip the dropped corners).  Stores are consecutive, every
+// lane has a pair in every round but the last, and one large splat is spread over the warp like
+// any other.  Also accumulates the tile counts (or the tile-key digit histograms of the tile
+// sort) in shared memory: each CTA loops over chunks of 256 ranks (grid-stride) and hands its
+// shared bins on once.
 template <bool COUNTS>
 __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
     const uint4 *__restrict__ info, const uint32_t *__restrict__ offsets, const uint32_t *count, uint32_t max_count,
@@ -354,7 +352,8 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
                 const uint32_t e = __shfl_sync(0xFFFFFFFFu, excl, src + step);
                 if (e <= r) src += step;
             }
-            const uint32_t sx = __shfl_sync(0xFFFFFFFFu, in.x, src), sw = __shfl_sync(0xFFFFFFFFu, w, src);
+            const uint32_t sx = __shfl_sync(0xFFFFFFFFu, in.x, src), swh = __shfl_sync(0xFFFFFFFFu, in.y, src);
+            const uint32_t sw = swh & 0xFFFFu;  // in.y: w | h << 16
             const uint32_t smask = __shfl_sync(0xFFFFFFFFu, in.z, src), sval = __shfl_sync(0xFFFFFFFFu, in.w, src);
             const float sinv = __shfl_sync(0xFFFFFFFFu, inv_w, src);
             const uint32_t sex = __shfl_sync(0xFFFFFFFFu, excl, src);
@@ -363,7 +362,7 @@ __global__ void __launch_bounds__(kBinThreads) bin_emit_kernel(
             if (r < run) {
                 const uint32_t local = r - sex;
                 // in.z: tiles kept of a rectangle of at most 16 (bit ty·w + tx); 0 = all of it
-                const uint32_t pos = smask ? nth_set_bit16(smask, local) : local;
+                const uint32_t pos = smask ? kept_tile_place(smask, sw, swh >> 16, local) : local;
                 // row = floor(pos / w), exact in float: pos < 2^24 and the error of 1/w is
                 // far below the 1/w gap between pos/w and the next integer
                 const uint32_t ty = (uint32_t)(((float)pos + 0.5f) * sinv), tx = pos - ty * sw;
