@@ -579,7 +579,8 @@ __global__ void __launch_bounds__(kPreThreads) preprocess_kernel(const __grid_co
     }
 
     // ---- per-instance vertex work (render.wesl:75-130), written at the Gaussian's index ----
-    if (vis && P.splats) write_splat<FMT>(u, g, pr, P.splats + i, P.binfo ? P.binfo + i : nullptr, P.tiles_x, P.tiles_y);
+    if (vis && P.splats)
+        write_splat<FMT>(u, g, pr, P.splats + i, P.binfo ? P.binfo + i : nullptr, P.tiles_x, P.tiles_y);
 
     // ---- global offset: warp 0 looks back over the predecessors' published counts ----
     __syncthreads();

@@ -190,8 +190,9 @@ __device__ __forceinline__ uint32_t look_back_digit(const uint64_t *flags, uint3
 // 8-byte pairs contiguous in the scatter.
 // MATCH: peers from one match.any instead of a ballot per digit bit.  Measured on GB300 with
 // 512-thread blocks, the ballots are the cheaper of the two for both depth keys (0.224 against
-// 0.247 ms for a 6M-key sort) and tile keys (0.29 against 0.40 ms), so match.any is a tuning
-// choice for the depth sort only.
+// 0.247 ms for a 6M-key sort) and tile keys (0.29 against 0.40 ms).  match.any is a tuning choice
+// of the depth sort, and the last pass of float depth keys, whose top digit takes a few values
+// per warp, ranks by it.
 // The pass of one block (`block`: the look-back tile; lower blocks are lower, earlier-dispatched
 // CTAs of the same launch).
 template <bool IN_PACKED, bool OUT_PACKED, bool MATCH>
@@ -358,9 +359,9 @@ __global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) sort_pass_kernel
 // owns the CTAs [block_base[v], block_base[v + 1]) and each of them runs the pass on a block of
 // that segment's pairs with the segment's own control block, digit offsets and look-back flags.
 // Pass 0 reads `data` and writes `alt`, pass 1 the reverse, so two passes leave the pairs in place.
-__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm) sort_segments_kernel(const SortSegment *__restrict__ segs,
-                                                                        const uint32_t *__restrict__ block_base,
-                                                                        uint32_t nseg, uint32_t pass) {
+__global__ void __launch_bounds__(kSortThreads, kSortCtasPerSm)
+    sort_segments_kernel(const SortSegment *__restrict__ segs, const uint32_t *__restrict__ block_base, uint32_t nseg,
+                         uint32_t pass) {
     uint32_t lo = 0, hi = nseg - 1;
     while (lo < hi) {
         const uint32_t mid = (lo + hi + 1) >> 1;
