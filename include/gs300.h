@@ -189,7 +189,7 @@ gs_status gs_radix_sort(uint32_t *keys, uint32_t *values, uint32_t max_count,
  * allocator and that therefore cannot hand this library a scratch buffer.  Same contract as
  * gs_radix_sort (stable, in place, bits [0, key_bits), device-side `count`), but its scratch is a
  * static device array inside the library: at most 1,048,576 (2^20) pairs per call, and every
- * device that loads the library holds about 19 MB for it until the process exits.  Larger
+ * device that loads the library holds about 18 MB for it until the process exits.  Larger
  * `max_count` returns GS_ERR_INVALID_ARG.  Calls of any size and key width up to that limit may
  * follow one another (the array is zero when the library loads and is then reused like any
  * caller scratch).  The first call on a device looks up the array's device address with that
