@@ -92,9 +92,12 @@ __device__ __forceinline__ void hist_add(uint32_t *h, uint32_t k, bool valid, co
 
 // Every CTA first clears its share of the flag-arena words this call must clear (the passes,
 // which are the arena's only readers, run after this kernel).
+// With `vals`, each CTA also asks L2 for the values of the keys it reads, which the first pass
+// reads next (the keys themselves arrive in L2 through this kernel's reads).
 __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restrict__ keys,
-                                                        const uint32_t *count, uint32_t max_count,
-                                                        const PassSplit sp, Ctrl *ctrl, uint64_t *arena) {
+                                                        const uint32_t *__restrict__ vals, const uint32_t *count,
+                                                        uint32_t max_count, const PassSplit sp, Ctrl *ctrl,
+                                                        uint64_t *arena) {
     __shared__ uint32_t h[1024];
     const uint32_t npasses = sp.n, hs = hist_stride(sp.n);
     uint32_t *gh = &ctrl->hist[0][0];
@@ -108,8 +111,14 @@ __global__ void __launch_bounds__(256) sort_hist_kernel(const uint32_t *__restri
     // Whole warps iterate together (bounds padded to the warp) so the ballots see 32 lanes.
     const uint32_t n4 = (n + 3u) / 4u;
     const uint32_t nr = (n4 + 31u) & ~31u;
+    const bool pf = vals && ((uintptr_t)vals & 15u) == 0;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nr; q += stride) {
         const uint32_t i0 = q * 4u;
+        if (pf && threadIdx.x == 0 && i0 < n) {
+            // this CTA's 4 x blockDim keys of the iteration start at i0 (a multiple of 16 bytes)
+            const uint32_t bytes = min(4u * 4u * blockDim.x, (n - i0) * 4u) & ~15u;
+            if (bytes) prefetch_l2_bulk(vals + i0, bytes);
+        }
         uint32_t k[4];
         if (vec && i0 + 4u <= n) {
             const uint4 v = *reinterpret_cast<const uint4 *>(keys + i0);
@@ -576,7 +585,7 @@ cudaError_t launch_sort(uint32_t *keys, uint32_t *vals, uint32_t max_count, cons
     uint32_t hist_blocks = (max_count + 256 * 4 * 4 - 1) / (256 * 4 * 4);
     if (hist_blocks > 152 * 8) hist_blocks = 152 * 8;
     if (tn.hist_blocks) hist_blocks = tn.hist_blocks < 152 * 8 ? tn.hist_blocks : 152 * 8;
-    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, count, max_count, sp, L.ctrl, L.flags);
+    sort_hist_kernel<<<hist_blocks, 256, 0, st>>>(keys, vals, count, max_count, sp, L.ctrl, L.flags);
     count_launches(1);
     // Keys of kDepthKeyBits are the render path's float depth keys (1 - ndc.z).
     if (tn.sort_match)
